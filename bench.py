@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Benchmark: accepted DP45 steps x N x batch per second on one GB300.
+
+Workload (default ``volcano200k``): the large on-the-fly volcano network,
+N=200000 oscillators, rank K=5, adjacency regenerated from Philox (-A) and never
+stored, coupling constant swept over c in {1,2,3,4,5} as a batch of 5
+trajectories sharing the network, normal frequencies (glibc rand, seed 1, -n),
+initial phases uniform in [0, pi) (seeded), t=50, output every dt=1,
+atol=1e-6, rtol=0.  One bench step = the whole integration of all 5
+trajectories from t=0 to t=50.  Synthetic inputs of that shape; nothing is read
+from disk.
+
+Arms:
+  --impl native (default): libkura through its C ABI.  ``value`` times the
+      integration with inputs already resident in HBM; ``e2e`` times the same
+      through host buffers (frequencies and phases copied in, order parameter and
+      final phases copied out, inside the timed region).
+  --impl reference: the reference's CPU path, i.e. the oracle's restatement of the
+      reference program (float32, reference arithmetic), on all host threads.
+
+Multi-GPU: each rank integrates its own instance (network seed 1 + rank) of the
+same workload; no collective on the data path (weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "volcano200k": dict(n=200000, k=5, coupling=1, cs=[1.0, 2.0, 3.0, 4.0, 5.0], normal=True, init=np.pi,
+                        t1=50.0, dt=1.0, atol=1e-6, rtol=0.0, shared_theta=True),
+    # the reference's default dense case (configs: N=5000, K=5, c=3, Cauchy, theta0=0, t=100, dt=1)
+    "dense5000": dict(n=5000, k=5, coupling=0, cs=[3.0], normal=False, init=0.0, t1=100.0, dt=1.0, atol=1e-6,
+                      rtol=0.0, shared_theta=True),
+    # the plain FP32 path at N=65536: 8 trajectories per pass over A, bounded horizon
+    "dense65536": dict(n=65536, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.5, dt=0.1,
+                       atol=1e-6, rtol=0.0, shared_theta=False),
+}
+# algorithmic bytes per accepted oscillator-step of the dominant kernel
+#   volcano: the DP45 state a step moves in the reference design (~150 B)
+#   dense:   6 RHS x 4N bytes of A per step, shared by the trajectories of one pass
+STATE_BYTES = 150.0
+
+
+def inputs(w, seed):
+    import kuramoto_gb300 as kg
+    n = w["n"]
+    _, om = kg.random_inputs(seed, n, 0.0, 1.0, w["normal"], gen_theta=False)
+    rng = np.random.default_rng(seed)
+    B = len(w["cs"])
+    if w["shared_theta"]:
+        th = (rng.random(n) * w["init"]).astype(np.float32)
+        thetas = [th] * B
+    else:
+        thetas = [(rng.random(n) * w["init"]).astype(np.float32) for _ in range(B)]
+    return thetas, om
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 2 + i and r[2 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_native(args, w):
+    import torch
+    import kuramoto_gb300 as kg
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    seed = 1 + rank
+    thetas, om = inputs(w, seed)
+    n, B = w["n"], len(w["cs"])
+    stream = torch.cuda.current_stream()
+    net = kg.Network(n, k=w["k"], coupling=w["coupling"], batch=B, seed=seed, atol=w["atol"], rtol=w["rtol"],
+                     dense_level=0, device=local, stream=stream.cuda_stream)
+    net.set_frequencies(om)
+    if w["coupling"] == 0:
+        net.generate_adjacency()
+    for b, c in enumerate(w["cs"]):
+        net.set_coupling(b, c)
+    dev_th = [torch.from_numpy(t).cuda() for t in thetas]
+    h0 = w["dt"] / 100
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+
+    def step_resident():
+        for b in range(B):
+            net.set_state_device(b, dev_th[b].data_ptr(), 0.0, h0)
+        net.set_horizon(w["t1"], w["dt"], True)
+        net.run()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step_resident()
+    # ---- value: inputs resident in HBM, L2 flushed between steps (outside the events)
+    st0 = net.stats()
+    barrier()
+    evs = []
+    with Clocks(local) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step_resident()
+            e1.record(stream)
+            evs.append((e0, e1))
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    st1 = net.stats()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    acc = st1["accepted"] * args.steps  # accepted steps of the last run, all trajectories
+    acc_per_step = st1["accepted"]
+    launches = st1["launches"] - st0["launches"]
+    kernel_ms = st1["kernel_ms"] - st0["kernel_ms"]
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    units = acc_per_step * n * args.steps * ws
+    value = units / (ms / 1e3)
+    orders = [net.order(b) for b in range(B)]
+
+    # ---- e2e: host buffers through the C ABI, copies inside the timed region
+    e2e_ms = 0.0
+    h2d = d2h = 0
+    th_out = np.zeros(n, np.float32)
+    for it in range(args.steps):
+        flush.zero_()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        net.set_frequencies(om)
+        for b in range(B):
+            net.set_state(b, thetas[b], 0.0, h0)
+        net.set_horizon(w["t1"], w["dt"], True)
+        net.run()
+        rs = [net.order(b) for b in range(B)]
+        finals = [net.state(b)[0] for b in range(B)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        if it == 0:
+            h2d = 4 * n + 4 * n * B
+            d2h = sum(4 * r.size for r in rs) + 4 * n * B
+    e2e_value = acc_per_step * n * args.steps * ws / (e2e_ms / 1e3)
+    net.close()
+    res = dict(value=value, ms=ms, wall=t_wall, kernel_ms=kernel_ms, launches=launches, acc_per_step=acc_per_step,
+               e2e_value=e2e_value, h2d=h2d, d2h=d2h, clocks=clk.summary(), orders=orders, thetas=thetas, om=om,
+               rank=rank, ws=ws, B=B)
+    return res
+
+
+def roofline(w, res, args):
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    src = "measured" if "hbm_gbs" in peaks else "fallback"
+    n = w["n"]
+    kernel_s = res["kernel_ms"] / 1e3 / max(res["launches"], 1)
+    acc_per_launch = res["acc_per_step"] * args.steps / max(res["launches"], 1)
+    if w["coupling"] == 1:
+        per_unit = STATE_BYTES
+        bytes_per_launch = per_unit * acc_per_launch * n
+    else:
+        per_unit = 24.0 * n / len(w["cs"])
+        bytes_per_launch = per_unit * acc_per_launch * n
+    achieved = bytes_per_launch / kernel_s / 1e9
+    traffic = None
+    try:
+        prof = _json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        t = prof.get(args.workload)
+        if t:
+            traffic = t["bytes_per_accepted_osc_step"] * acc_per_launch * n
+    except Exception:
+        pass
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": src,
+            "bytes_per_unit": per_unit, "kernel_ms_per_launch": round(kernel_s * 1e3, 3)}
+
+
+def cpu_baseline(w, om, thetas, threads, sample_steps=None):
+    from oracle import kora
+    n = w["n"]
+    t0 = time.perf_counter()
+    steps = 0
+    for b, c in enumerate(w["cs"]):
+        r = kora.run(thetas[b], om, k=w["k"], c1=c, onthefly=w["coupling"] == 1, seed=1, fp64=False, t1=w["t1"],
+                     dt=w["dt"], atol=w["atol"], rtol=w["rtol"], threads=threads)
+        steps += r.steps
+    el = time.perf_counter() - t0
+    return steps * n / el, el, steps
+
+
+def r_error_vs_fp64(w, om, theta, c, gpu_order, threads, t1=3.0):
+    """max |r_gpu - r_fp64| over the first outputs (the FP64 oracle on a bounded horizon)."""
+    from oracle import kora
+    r = kora.run(theta, om, k=w["k"], c1=c, onthefly=w["coupling"] == 1, seed=1, fp64=True, t1=t1, dt=w["dt"],
+                 atol=w["atol"], rtol=w["rtol"], threads=threads)
+    m = min(r.order.size, gpu_order.size)
+    return float(np.max(np.abs(r.order[:m] - gpu_order[:m])))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--workload", default="volcano200k", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    ws, rank, local = dist_env()
+    n, B = w["n"], len(w["cs"])
+    config = {"workload": args.workload, "n": n, "k": w["k"], "coupling": "volcano-regenerated" if w["coupling"] else
+              "dense", "batch": B, "c": w["cs"], "t1": w["t1"], "dt": w["dt"], "atol": w["atol"],
+              "rtol": w["rtol"], "frequencies": "normal (glibc rand, seed 1)" if w["normal"] else "cauchy",
+              "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas" if ws > 1 else "single"}
+    metric = "accepted DP45 steps x N x batch / s"
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import kora
+        import kuramoto_gb300 as kg  # host RNG only (glibc rand), no GPU use
+        thetas, om = inputs(w, 1)
+        for _ in range(args.warmup):
+            cpu_baseline(w, om, thetas, threads)
+        tot_units = 0.0
+        tot_s = 0.0
+        for _ in range(args.steps):
+            v, el, steps = cpu_baseline(w, om, thetas, threads)
+            tot_units += steps * n
+            tot_s += el
+        value = tot_units / tot_s
+        line = {"impl": "reference", "metric": metric, "value": value, "unit": "osc-steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_s / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": value, "unit": "osc-steps/s", "cores": threads, "kind": "port",
+                                 "sample": "whole workload per step (5 trajectories to t=%g), float32 oracle "
+                                           "restating the reference program, OpenMP" % w["t1"]},
+                "e2e": {"value": value, "unit": "osc-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    res = run_native(args, w)
+    if rank != 0:
+        return
+    line = {"metric": metric, "value": res["value"], "unit": "osc-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config}
+    line["e2e"] = {"value": res["e2e_value"], "unit": "osc-steps/s", "h2d_bytes_per_step": res["h2d"],
+                   "d2h_bytes_per_step": res["d2h"]}
+    # launches of our kernels per step: B state uploads + 1 persistent launch
+    line["gpu_launches"] = (B + 1) * args.steps
+    line["roofline"] = roofline(w, res, args)
+    line["clocks"] = res["clocks"]
+    line["accepted_steps_per_run"] = res["acc_per_step"]
+    if not args.no_cpu:
+        v, el, steps = cpu_baseline(w, res["om"], res["thetas"], threads)
+        line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
+                                "sample": "whole workload (5 trajectories to t=%g, %d accepted steps, %.1f s), "
+                                          "float32 oracle restating the reference program" % (w["t1"], steps, el)}
+        ci = len(w["cs"]) // 2
+        line["r_err_vs_fp64"] = r_error_vs_fp64(w, res["om"], res["thetas"][ci], w["cs"][ci], res["orders"][ci],
+                                                threads)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

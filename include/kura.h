@@ -1,0 +1,131 @@
+/* kura.h -- C ABI of the GB300 Kuramoto DP45 integrator (libkura.so).
+ *
+ * The reference program (znicolaou/kuramoto) has no library interface: its
+ * integrator is the static-state C ABI of dp45.h, driven by host callbacks
+ * (dydt once per stage, step_eval once per accepted step), and its user-facing
+ * surface is the `kuramoto` command line plus the FILEBASE files.  This header
+ * replaces that internal ABI with explicit handles.  Each entry point names the
+ * reference code it stands in for.
+ *
+ * Conventions: every call returns KURA_OK (0) or a negative KURA_ERR_* code;
+ * kura_last_error() gives a message for the calling thread.  All pointers are
+ * host pointers unless the name ends in _device.  Calls on one handle are not
+ * thread-safe.  Oscillator arrays are float32; adjacency rows are contiguous
+ * (row i at adj + i*n), which is the buffer the reference hands to cuBLAS
+ * (column-major with OP_T, kuramoto.cu:113-114).
+ */
+#ifndef KURA_H
+#define KURA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KURA_OK 0
+#define KURA_ERR_INVALID (-1)         /* bad argument or call order */
+#define KURA_ERR_CUDA (-2)            /* CUDA runtime error */
+#define KURA_ERR_NOMEM (-3)           /* device allocation failed */
+#define KURA_ERR_BARRIER_TIMEOUT (-4) /* a grid barrier of the persistent kernel gave up */
+#define KURA_ERR_STEP_UNDERFLOW (-5)  /* step size fell below 1e-14 * max(1,|t|) */
+#define KURA_ERR_NONFINITE (-6)       /* error norm became NaN or infinite */
+#define KURA_ERR_UNSUPPORTED (-7)     /* configuration outside the built kernels */
+#define KURA_ERR_CALLBACK (-8)        /* an observer callback returned non-zero */
+
+#define KURA_COUPLING_DENSE 0   /* adjacency stored in HBM (reference default) */
+#define KURA_COUPLING_VOLCANO 1 /* rank-K volcano factor regenerated from Philox (reference -A) */
+
+typedef struct kura_handle kura_handle;
+
+/* Network and integrator settings; the reference flag each field replaces is given. */
+typedef struct kura_config {
+  int64_t n;           /* -N oscillators */
+  int32_t k;           /* -K volcano rank */
+  int32_t coupling;    /* KURA_COUPLING_DENSE or KURA_COUPLING_VOLCANO (-A) */
+  int32_t batch;       /* trajectories sharing omega and the adjacency (1 = the reference) */
+  int32_t seed;        /* -s Philox seed of the volcano factor */
+  double atol;         /* -a */
+  double rtol;         /* -r */
+  int32_t fixed_step;  /* -F */
+  int32_t device;      /* -g */
+  int32_t dense_level; /* -D: 0 order only; >=1 adds phases and step times; >=2 adds couplings */
+  int32_t reserved0;
+  void* stream;        /* cudaStream_t for every launch and copy (NULL: a stream owned by the handle) */
+} kura_config;
+
+typedef struct kura_stats {
+  int64_t accepted;    /* accepted steps, summed over trajectories */
+  int64_t rejected;    /* rejected attempts, summed over trajectories */
+  int64_t launches;    /* persistent-kernel launches */
+  int64_t barriers;    /* grid barriers executed (all launches) */
+  double kernel_ms;    /* device time of the persistent launches (CUDA events) */
+  int32_t grid;        /* CTAs of the persistent kernel */
+  int32_t block;       /* threads per CTA */
+} kura_stats;
+
+/* Per-record observer callbacks, called from kura_run on the calling thread, in
+ * order, after each persistent launch is drained.  Return non-zero to abort.
+ * on_step mirrors step_eval's per-step work (kuramoto.cu:169-188); on_output the
+ * per-t_eval work (kuramoto.cu:212-234); theta / couplings are NULL when the
+ * dense level does not ask for them.  on_chunk is called after each launch with
+ * the current phases (for checkpoint files such as fs.dat). */
+typedef struct kura_callbacks {
+  void* user;
+  int (*on_step)(void* user, int32_t traj, double t, double h, int64_t step);
+  int (*on_output)(void* user, int32_t traj, int64_t index, double t_eval, float r, const float* theta,
+                   const float* couplings);
+  int (*on_chunk)(void* user, int32_t traj, double t, double h, const float* theta);
+} kura_callbacks;
+
+/* replaces dp45_init (dp45.h:8) and the allocations of main (kuramoto.cu:442-457) */
+int kura_create(const kura_config* cfg, kura_handle** out);
+/* replaces dp45_destroy (dp45.h:10) and main's frees (kuramoto.cu:659-675) */
+void kura_destroy(kura_handle* h);
+const char* kura_last_error(void);
+/* device memory the handle holds, in bytes (the reference prints its estimate, kuramoto.cu:424-433) */
+int kura_memory_required(const kura_config* cfg, int64_t* bytes);
+
+/* omega upload (kuramoto.cu:552) */
+int kura_set_frequencies(kura_handle* h, const float* omega, int64_t n);
+/* adjacency from a file (-R, kuramoto.cu:559-566); row-major n x n */
+int kura_set_adjacency(kura_handle* h, const float* adj, int64_t n);
+/* volcano adjacency A = (1/N) sum_m (-1)^m u_m u_m^T (getadj, kuramoto.cu:128-161) */
+int kura_generate_adjacency(kura_handle* h);
+/* adjacency download for adj.dat (kuramoto.cu:573-578) */
+int kura_get_adjacency(kura_handle* h, float* adj, int64_t n);
+/* coupling constant of one trajectory (-c, tot_kuramoto's c1, kuramoto.cu:42-47) */
+int kura_set_coupling(kura_handle* h, int32_t traj, float c);
+/* phases, time and step of one trajectory (random start or -R reload, kuramoto.cu:459-506) */
+int kura_set_state(kura_handle* h, int32_t traj, const float* theta, double t, double step);
+int kura_set_state_device(kura_handle* h, int32_t traj, const float* theta_device, double t, double step);
+/* output grid t_eval = dt*n, n = int(t0/dt)+1 .. int(t1/dt), and the end time
+ * (kuramoto.cu:543-550); initial_record = 1 writes r(theta0) (and theta0,
+ * couplings) first, as a fresh start does (kuramoto.cu:587-626) */
+int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t initial_record);
+
+/* integrate every trajectory to t1 (dp45_run with step_eval, dp45.cu:148-164) */
+int kura_run(kura_handle* h, const kura_callbacks* cb);
+
+/* current phases (unwrapped), time and step of one trajectory */
+int kura_get_state(kura_handle* h, int32_t traj, float* theta, double* t, double* step);
+/* order parameter records of one trajectory since kura_set_horizon (order.dat) */
+int kura_get_order(kura_handle* h, int32_t traj, float* r, int64_t cap, int64_t* count);
+/* end-of-run record of fs.dat: phases at the last output time, evaluated after the
+ * FSAL copy as the reference does (kuramoto.cu:630-647), and the couplings there */
+int kura_final_record(kura_handle* h, int32_t traj, float* theta, float* couplings, double* t, double* step);
+/* right-hand side dtheta/dt and couplings [A cos, A sin] interleaved at theta (dydt, kuramoto.cu:118-126) */
+int kura_rhs(kura_handle* h, int32_t traj, const float* theta, float* dtheta, float* couplings);
+int kura_get_stats(kura_handle* h, kura_stats* st);
+
+/* host random inputs with glibc rand(): theta0 uniform in [-init/2, init/2] then
+ * Cauchy or normal frequencies (kuramoto.cu:416, 495-541) */
+int kura_random_inputs(int32_t seed, int64_t n, float init, float freq, int32_t normal, int32_t gen_theta,
+                       int32_t gen_omega, float* theta0, float* omega);
+/* Philox4x32-10 volcano factor bits as +/-1 int8 at m*n+i (kuramoto.cu:62-101, 128-135), on the device */
+int kura_volcano_factor(int32_t seed, int64_t n, int32_t k, int8_t* u);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,608 @@
+// kura_api.cu -- C ABI of libkura (declared in include/kura.h).
+//
+// Owns the device buffers of one network and its batch of trajectories, launches
+// the persistent DP45 kernel, drains its output rings and calls the observer
+// callbacks.  Stands in for dp45_init/dp45_run/dp45_eval/dp45_destroy
+// (dp45.h:7-11) and for the device-side parts of the reference main
+// (kuramoto.cu:409-457, 552-585, 628-647).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "kura.h"
+#include "kura_kernels.cuh"
+
+using kura::TrajG;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+#define CU(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(e_ == cudaErrorMemoryAllocation ? KURA_ERR_NOMEM : KURA_ERR_CUDA,           \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+  } while (0)
+
+struct kura_handle {
+  kura_config cfg{};
+  int n = 0, ld = 0, B = 0, K = 0, bmax = 1, kmax = 8, coupling = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // device
+  float* omega = nullptr;
+  float* adj = nullptr;
+  float* ph_hi = nullptr;
+  float* ph_lo = nullptr;
+  long long* ph_w = nullptr;
+  float* g = nullptr;
+  float2* xbuf = nullptr;
+  float* part = nullptr;
+  unsigned* bar = nullptr;
+  int* err = nullptr;
+  TrajG* traj = nullptr;
+  float* t_eval = nullptr;
+  float* out_r = nullptr;
+  int* out_idx = nullptr;
+  float* out_theta = nullptr;
+  float* out_coup = nullptr;
+  double* log_t = nullptr;
+  double* log_h = nullptr;
+  float* fin_theta = nullptr;
+  float* fin_coup = nullptr;
+  long long* counters = nullptr;
+  int ring = 0, ring_alloc = 0, ring_dl = -1, log_cap = 0, n_eval = 0, t_eval_alloc = 0;
+  double dt = 1, t1 = 0;
+  int grid = 1, rows = 1;
+  size_t smem = 0;
+  // host
+  std::vector<TrajG> htraj;
+  std::vector<std::vector<float>> order;
+  std::vector<float> c1;
+  std::vector<float> t_eval_h;
+  std::vector<double> t0;
+  bool omega_set = false, adj_set = false, horizon_set = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  kura_stats stats{};
+};
+
+extern "C" const char* kura_last_error(void) { return g_err.c_str(); }
+
+static int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+static void plan(const kura_config* c, int* ld, int* bmax, int* kmax) {
+  *ld = (int)((c->n + 31) / 32 * 32);
+  *bmax = c->batch <= 1 ? 1 : 8;
+  *kmax = c->k <= 8 ? 8 : 32;
+}
+
+static int validate(const kura_config* c) {
+  if (!c) return fail(KURA_ERR_INVALID, "config is NULL");
+  if (c->n < 1 || c->n > (1LL << 30)) return fail(KURA_ERR_INVALID, "n must be in [1, 2^30]");
+  if (c->batch < 1) return fail(KURA_ERR_INVALID, "batch must be >= 1");
+  if (c->batch > 8) return fail(KURA_ERR_UNSUPPORTED, "batch > 8 is not built into the persistent kernel");
+  if (c->k < 0) return fail(KURA_ERR_INVALID, "k must be >= 0");
+  if (c->coupling != KURA_COUPLING_DENSE && c->coupling != KURA_COUPLING_VOLCANO)
+    return fail(KURA_ERR_INVALID, "unknown coupling");
+  if (c->coupling == KURA_COUPLING_VOLCANO && c->k > 32)
+    return fail(KURA_ERR_UNSUPPORTED, "regenerated volcano coupling supports k <= 32");
+  if (c->coupling == KURA_COUPLING_VOLCANO && (long long)c->k * c->n >= (1LL << 62))
+    return fail(KURA_ERR_INVALID, "k*n too large");
+  if (!(c->atol > 0) && !c->fixed_step) return fail(KURA_ERR_INVALID, "atol must be > 0");
+  if (c->rtol < 0) return fail(KURA_ERR_INVALID, "rtol must be >= 0");
+  return KURA_OK;
+}
+
+extern "C" int kura_memory_required(const kura_config* c, int64_t* bytes) {
+  int rc = validate(c);
+  if (rc) return rc;
+  int ld, bmax, kmax;
+  plan(c, &ld, &bmax, &kmax);
+  long long B = c->batch, n = ld;
+  long long b = 4 * n;                                   // omega
+  if (c->coupling == KURA_COUPLING_DENSE) b += 4LL * c->n * n;
+  b += 2 * B * n * (4 + 4 + 8);                          // phases
+  b += 7 * B * n * 4;                                    // slopes
+  b += 2 * B * n * 8;                                    // exchange
+  b += B * n * 4 * 3;                                    // end record
+  *bytes = b;
+  return KURA_OK;
+}
+
+extern "C" void kura_destroy(kura_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->cfg.device);
+  void* ptrs[] = {h->omega, h->adj, h->ph_hi, h->ph_lo, h->ph_w, h->g, h->xbuf, h->part, h->bar, h->err,
+                  h->traj, h->t_eval, h->out_r, h->out_idx, h->out_theta, h->out_coup, h->log_t, h->log_h,
+                  h->fin_theta, h->fin_coup, h->counters};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+template <typename T> static cudaError_t dalloc(T** p, size_t count) {
+  cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+  if (e == cudaSuccess) e = cudaMemset(*p, 0, std::max<size_t>(count, 1) * sizeof(T));
+  return e;
+}
+
+extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
+  if (!out) return fail(KURA_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  int ndev = 0;
+  CU(cudaGetDeviceCount(&ndev));
+  if (cfg->device < 0 || cfg->device >= ndev) return fail(KURA_ERR_INVALID, "device index out of range");
+  CU(cudaSetDevice(cfg->device));
+  auto* h = new kura_handle();
+  h->cfg = *cfg;
+  h->n = (int)cfg->n;
+  h->B = cfg->batch;
+  h->K = cfg->k;
+  h->coupling = cfg->coupling;
+  plan(cfg, &h->ld, &h->bmax, &h->kmax);
+  auto bail = [&](int code) {
+    kura_destroy(h);
+    return code;
+  };
+#define CUH(call)                                                                               \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return bail(fail(e_ == cudaErrorMemoryAllocation ? KURA_ERR_NOMEM : KURA_ERR_CUDA,        \
+                       std::string(#call) + ": " + cudaGetErrorString(e_)));                    \
+  } while (0)
+  if (cfg->stream) {
+    h->stream = (cudaStream_t)cfg->stream;
+  } else {
+    CUH(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+  }
+  CUH(cudaEventCreate(&h->ev0));
+  CUH(cudaEventCreate(&h->ev1));
+
+  // grid: one or more CTAs per SM, all co-resident (cooperative launch)
+  int dev = cfg->device, sms = 0, coop = 0;
+  CUH(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CUH(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) return bail(fail(KURA_ERR_UNSUPPORTED, "device lacks cooperative launch"));
+  int G = sms;
+  int rows = ceil_div(h->n, G);
+  int bps = 0;
+  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows));
+  if (bps < 1) return bail(fail(KURA_ERR_UNSUPPORTED, "persistent kernel does not fit on an SM"));
+  G = sms * std::min(bps, 1);
+  G = std::min(G, std::max(1, ceil_div(h->n, 64)));
+  rows = ceil_div(h->n, G);
+  G = ceil_div(h->n, rows);
+  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows));
+  if (bps < 1) return bail(fail(KURA_ERR_UNSUPPORTED, "persistent kernel shared memory exceeds an SM"));
+  h->grid = G;
+  h->rows = rows;
+
+  size_t ld = h->ld, B = h->B;
+  CUH(dalloc(&h->omega, ld));
+  if (h->coupling == KURA_COUPLING_DENSE) CUH(dalloc(&h->adj, (size_t)h->n * ld));
+  CUH(dalloc(&h->ph_hi, 2 * B * ld));
+  CUH(dalloc(&h->ph_lo, 2 * B * ld));
+  CUH(dalloc(&h->ph_w, 2 * B * ld));
+  CUH(dalloc(&h->g, 7 * B * ld));
+  CUH(dalloc(&h->xbuf, 2 * B * ld));
+  CUH(dalloc(&h->part, 2 * (size_t)G * B * kura::PW_MAX));
+  CUH(dalloc(&h->bar, 4));
+  CUH(dalloc(&h->err, 4));
+  CUH(dalloc(&h->traj, B));
+  CUH(dalloc(&h->fin_theta, B * ld));
+  CUH(dalloc(&h->fin_coup, 2 * B * ld));
+  CUH(dalloc(&h->counters, 4));
+  h->log_cap = 4096;
+  CUH(dalloc(&h->log_t, B * (size_t)h->log_cap));
+  CUH(dalloc(&h->log_h, B * (size_t)h->log_cap));
+  h->htraj.assign(B, TrajG{});
+  for (auto& T : h->htraj) {
+    T.status = 1;  // no state yet
+    T.c1 = 0.f;
+  }
+  h->c1.assign(B, 0.f);
+  h->t0.assign(B, 0.0);
+  h->order.assign(B, {});
+  h->stats.grid = G;
+  h->stats.block = kura::KT;
+  *out = h;
+  return KURA_OK;
+#undef CUH
+}
+
+static int check_traj(kura_handle* h, int traj) {
+  if (!h) return fail(KURA_ERR_INVALID, "handle is NULL");
+  if (traj < 0 || traj >= h->B) return fail(KURA_ERR_INVALID, "trajectory index out of range");
+  return KURA_OK;
+}
+
+extern "C" int kura_set_frequencies(kura_handle* h, const float* omega, int64_t n) {
+  if (!h || !omega) return fail(KURA_ERR_INVALID, "NULL argument");
+  if (n != h->n) return fail(KURA_ERR_INVALID, "frequency count differs from n");
+  CU(cudaSetDevice(h->cfg.device));
+  CU(cudaMemcpyAsync(h->omega, omega, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  h->omega_set = true;
+  return KURA_OK;
+}
+
+extern "C" int kura_set_adjacency(kura_handle* h, const float* adj, int64_t n) {
+  if (!h || !adj) return fail(KURA_ERR_INVALID, "NULL argument");
+  if (h->coupling != KURA_COUPLING_DENSE) return fail(KURA_ERR_INVALID, "adjacency is regenerated (volcano coupling)");
+  if (n != h->n) return fail(KURA_ERR_INVALID, "adjacency size differs from n");
+  CU(cudaSetDevice(h->cfg.device));
+  CU(cudaMemcpy2DAsync(h->adj, sizeof(float) * h->ld, adj, sizeof(float) * n, sizeof(float) * n, n,
+                       cudaMemcpyHostToDevice, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  h->adj_set = true;
+  return KURA_OK;
+}
+
+extern "C" int kura_generate_adjacency(kura_handle* h) {
+  if (!h) return fail(KURA_ERR_INVALID, "handle is NULL");
+  if (h->coupling != KURA_COUPLING_DENSE) return fail(KURA_ERR_INVALID, "adjacency is regenerated (volcano coupling)");
+  CU(cudaSetDevice(h->cfg.device));
+  int words = (h->K + 31) / 32;
+  uint32_t* bits = nullptr;
+  if (words > 0) {
+    CU(cudaMallocAsync((void**)&bits, sizeof(uint32_t) * (size_t)words * h->n, h->stream));
+    CU(kura::launch_volcano_words(h->cfg.seed, h->n, h->K, words, bits, h->stream));
+  }
+  CU(kura::launch_volcano_adjacency(bits, h->n, h->K, words, h->ld, h->adj, h->stream));
+  if (bits) CU(cudaFreeAsync(bits, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  h->adj_set = true;
+  return KURA_OK;
+}
+
+extern "C" int kura_get_adjacency(kura_handle* h, float* adj, int64_t n) {
+  if (!h || !adj) return fail(KURA_ERR_INVALID, "NULL argument");
+  if (h->coupling != KURA_COUPLING_DENSE || !h->adj_set) return fail(KURA_ERR_INVALID, "no stored adjacency");
+  if (n != h->n) return fail(KURA_ERR_INVALID, "adjacency size differs from n");
+  CU(cudaSetDevice(h->cfg.device));
+  CU(cudaMemcpy2DAsync(adj, sizeof(float) * n, h->adj, sizeof(float) * h->ld, sizeof(float) * n, n,
+                       cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  return KURA_OK;
+}
+
+extern "C" int kura_set_coupling(kura_handle* h, int32_t traj, float c) {
+  int rc = check_traj(h, traj);
+  if (rc) return rc;
+  h->c1[traj] = c;
+  h->htraj[traj].c1 = c;
+  return KURA_OK;
+}
+
+static int set_state_common(kura_handle* h, int traj, const float* dev_theta, double t, double step) {
+  size_t off = (size_t)traj * h->ld;  // physical buffer 0
+  CU(kura::launch_init_state(dev_theta, h->n, h->ld, h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  TrajG& T = h->htraj[traj];
+  float c = T.c1;
+  T = TrajG{};
+  T.c1 = c;
+  T.t = t;
+  T.h = step;
+  T.t_last = t;
+  T.t1 = t;
+  T.status = 0;
+  T.need_k1 = 1;
+  T.need_init = 0;
+  h->horizon_set = false;
+  return KURA_OK;
+}
+
+extern "C" int kura_set_state(kura_handle* h, int32_t traj, const float* theta, double t, double step) {
+  int rc = check_traj(h, traj);
+  if (rc) return rc;
+  if (!theta) return fail(KURA_ERR_INVALID, "theta is NULL");
+  if (!(step > 0)) return fail(KURA_ERR_INVALID, "step must be > 0");
+  CU(cudaSetDevice(h->cfg.device));
+  float* tmp = h->fin_theta + (size_t)traj * h->ld;
+  CU(cudaMemcpyAsync(tmp, theta, sizeof(float) * h->n, cudaMemcpyHostToDevice, h->stream));
+  return set_state_common(h, traj, tmp, t, step);
+}
+
+extern "C" int kura_set_state_device(kura_handle* h, int32_t traj, const float* theta_device, double t,
+                                     double step) {
+  int rc = check_traj(h, traj);
+  if (rc) return rc;
+  if (!theta_device) return fail(KURA_ERR_INVALID, "theta is NULL");
+  if (!(step > 0)) return fail(KURA_ERR_INVALID, "step must be > 0");
+  CU(cudaSetDevice(h->cfg.device));
+  return set_state_common(h, traj, theta_device, t, step);
+}
+
+extern "C" int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t initial_record) {
+  if (!h) return fail(KURA_ERR_INVALID, "handle is NULL");
+  if (!(dt > 0)) return fail(KURA_ERR_INVALID, "dt must be > 0");
+  for (int b = 0; b < h->B; ++b)
+    if (h->htraj[b].status != 0 || h->htraj[b].need_k1 != 1)
+      return fail(KURA_ERR_INVALID, "set the state of every trajectory before the horizon");
+  for (int b = 1; b < h->B; ++b)
+    if (h->htraj[b].t != h->htraj[0].t) return fail(KURA_ERR_INVALID, "trajectories must start at the same time");
+  CU(cudaSetDevice(h->cfg.device));
+  // t_eval = dt*n for n = int(t0/dt)+1 .. int(t1/dt), in float like the reference
+  float t0f = (float)h->htraj[0].t, dtf = (float)dt, t1f = (float)t1;
+  int n0 = int(t0f / dtf) + 1, n1 = int(t1f / dtf) + 1;
+  h->t_eval_h.clear();
+  for (int n = n0; n < n1; ++n) h->t_eval_h.push_back(dtf * n);
+  h->n_eval = (int)h->t_eval_h.size();
+  h->dt = dt;
+  h->t1 = t1;
+  if (h->n_eval > h->t_eval_alloc || !h->t_eval) {
+    if (h->t_eval) cudaFree(h->t_eval);
+    h->t_eval = nullptr;
+    CU(dalloc(&h->t_eval, h->t_eval_h.size()));
+    h->t_eval_alloc = h->n_eval;
+  }
+  if (h->n_eval)
+    CU(cudaMemcpyAsync(h->t_eval, h->t_eval_h.data(), sizeof(float) * h->n_eval, cudaMemcpyHostToDevice, h->stream));
+  // output ring: every record when only r is kept, else bounded by a 2 GiB budget
+  int dl = h->cfg.dense_level;
+  long long per = (long long)h->B * h->ld * 4 * ((dl >= 1 ? 1 : 0) + (dl >= 2 ? 2 : 0));
+  long long want = (long long)h->n_eval + 2;
+  long long ring = want;
+  if (per > 0) ring = std::min<long long>(want, std::max<long long>(4, (2LL << 30) / per));
+  if (ring > h->ring_alloc || dl != h->ring_dl) {
+    for (void* p : {(void*)h->out_r, (void*)h->out_idx, (void*)h->out_theta, (void*)h->out_coup})
+      if (p) cudaFree(p);
+    h->out_r = nullptr; h->out_idx = nullptr; h->out_theta = nullptr; h->out_coup = nullptr;
+    CU(dalloc(&h->out_r, (size_t)h->B * ring));
+    CU(dalloc(&h->out_idx, (size_t)h->B * ring));
+    if (dl >= 1) CU(dalloc(&h->out_theta, (size_t)h->B * ring * h->ld));
+    if (dl >= 2) CU(dalloc(&h->out_coup, (size_t)h->B * ring * 2 * h->ld));
+    h->ring_alloc = (int)ring;
+    h->ring_dl = dl;
+  }
+  h->ring = h->ring_alloc;
+  for (int b = 0; b < h->B; ++b) {
+    TrajG& T = h->htraj[b];
+    T.t1 = t1;
+    T.eval_i = 0;
+    T.eval_end = 0;
+    T.need_init = initial_record ? 1 : 0;
+    T.out_count = 0;
+    T.log_count = 0;
+    h->order[b].clear();
+    h->t0[b] = T.t;
+  }
+  h->horizon_set = true;
+  return KURA_OK;
+}
+
+static int launch(kura_handle* h, int mode, bool log_steps) {
+  kura::KParams p{};
+  p.n = h->n; p.ld = h->ld; p.batch = h->B; p.k = h->K; p.coupling = h->coupling;
+  p.dense_level = h->cfg.dense_level; p.fixed = h->cfg.fixed_step; p.rows = h->rows; p.seed = h->cfg.seed;
+  p.mode = mode;
+  p.omega = h->omega; p.adj = h->adj;
+  p.ph_hi = h->ph_hi; p.ph_lo = h->ph_lo; p.ph_w = h->ph_w; p.g = h->g; p.xbuf = h->xbuf; p.part = h->part;
+  p.bar = h->bar; p.err = h->err; p.traj = h->traj;
+  p.t_eval = h->t_eval; p.n_eval = h->n_eval;
+  p.atol = h->cfg.atol; p.rtol = h->cfg.rtol; p.dt = h->dt;
+  p.out_r = h->out_r; p.out_idx = h->out_idx; p.out_theta = h->out_theta; p.out_coup = h->out_coup;
+  p.ring = h->ring;
+  p.log_t = h->log_t; p.log_h = h->log_h; p.log_cap = log_steps ? h->log_cap : 0;
+  p.max_attempts = -1;
+  const char* to = getenv("KURA_BARRIER_TIMEOUT_MS");
+  double ms = to ? atof(to) : 20000.0;
+  p.timeout_ns = (unsigned long long)(ms * 1e6);
+  const char* extra = getenv("KURA_TEST_BARRIER_EXTRA");
+  p.bar_extra = extra ? (unsigned)atoi(extra) : 0u;
+  p.fin_theta = h->fin_theta; p.fin_coup = h->fin_coup;
+  p.counters = h->counters;
+  CU(cudaMemcpyAsync(h->traj, h->htraj.data(), sizeof(TrajG) * h->B, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaMemsetAsync(h->bar, 0, sizeof(unsigned), h->stream));
+  CU(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
+  CU(cudaEventRecord(h->ev0, h->stream));
+  CU(kura::launch_persistent(p, h->grid, h->bmax, h->kmax, h->smem, h->stream));
+  CU(cudaEventRecord(h->ev1, h->stream));
+  int err = 0;
+  CU(cudaMemcpyAsync(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(h->htraj.data(), h->traj, sizeof(TrajG) * h->B, cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  float ms_k = 0;
+  CU(cudaEventElapsedTime(&ms_k, h->ev0, h->ev1));
+  h->stats.kernel_ms += ms_k;
+  h->stats.launches++;
+  if (err) return fail(err, err == KURA_ERR_BARRIER_TIMEOUT ? "grid barrier timed out" : "persistent kernel aborted");
+  return KURA_OK;
+}
+
+extern "C" int kura_run(kura_handle* h, const kura_callbacks* cb) {
+  if (!h) return fail(KURA_ERR_INVALID, "handle is NULL");
+  if (!h->omega_set) return fail(KURA_ERR_INVALID, "frequencies not set");
+  if (h->coupling == KURA_COUPLING_DENSE && !h->adj_set) return fail(KURA_ERR_INVALID, "adjacency not set");
+  if (!h->horizon_set) return fail(KURA_ERR_INVALID, "horizon not set (kura_set_horizon after kura_set_state)");
+  CU(cudaSetDevice(h->cfg.device));
+  const bool log_steps = cb && cb->on_step;
+  std::vector<float> rbuf, thbuf, cpbuf;
+  std::vector<int> ibuf;
+  std::vector<double> lt, lh;
+  std::vector<long long> step_no(h->B, 0);
+  for (int b = 0; b < h->B; ++b) step_no[b] = h->htraj[b].accepted;
+  int stall = 0;
+  while (true) {
+    long long before = 0;
+    for (auto& T : h->htraj) before += T.accepted + T.rejected + T.out_count + T.eval_i;
+    int rc = launch(h, kura::MODE_INTEGRATE, log_steps);
+    if (rc) return rc;
+    // drain (order.dat, thetas.dat, couplings.dat, times.dat records)
+    for (int b = 0; b < h->B; ++b) {
+      TrajG& T = h->htraj[b];
+      int cnt = T.out_count;
+      if (cnt > 0) {
+        rbuf.resize(cnt);
+        ibuf.resize(cnt);
+        CU(cudaMemcpy(rbuf.data(), h->out_r + (size_t)b * h->ring, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(ibuf.data(), h->out_idx + (size_t)b * h->ring, sizeof(int) * cnt, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < cnt; ++q) h->order[b].push_back(rbuf[q]);
+        if (cb && cb->on_output) {
+          int dl = h->cfg.dense_level;
+          if (dl >= 1) {
+            thbuf.resize((size_t)cnt * h->ld);
+            CU(cudaMemcpy(thbuf.data(), h->out_theta + (size_t)b * h->ring * h->ld, sizeof(float) * cnt * h->ld,
+                          cudaMemcpyDeviceToHost));
+          }
+          if (dl >= 2) {
+            cpbuf.resize((size_t)cnt * 2 * h->ld);
+            CU(cudaMemcpy(cpbuf.data(), h->out_coup + (size_t)b * h->ring * 2 * h->ld,
+                          sizeof(float) * cnt * 2 * h->ld, cudaMemcpyDeviceToHost));
+          }
+          for (int q = 0; q < cnt; ++q) {
+            int idx = ibuf[q];
+            double te = idx < 0 ? h->t0[b] : (double)h->t_eval_h[idx];
+            const float* th = dl >= 1 ? thbuf.data() + (size_t)q * h->ld : nullptr;
+            const float* cp = dl >= 2 ? cpbuf.data() + (size_t)q * 2 * h->ld : nullptr;
+            if (cb->on_output(cb->user, b, idx, te, rbuf[q], th, cp)) return fail(KURA_ERR_CALLBACK, "on_output aborted");
+          }
+        }
+      }
+      if (log_steps && T.log_count > 0) {
+        int lc = std::min(T.log_count, h->log_cap);
+        lt.resize(lc);
+        lh.resize(lc);
+        CU(cudaMemcpy(lt.data(), h->log_t + (size_t)b * h->log_cap, sizeof(double) * lc, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(lh.data(), h->log_h + (size_t)b * h->log_cap, sizeof(double) * lc, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < lc; ++q)
+          if (cb->on_step(cb->user, b, lt[q], lh[q], ++step_no[b])) return fail(KURA_ERR_CALLBACK, "on_step aborted");
+      }
+      T.out_count = 0;
+      T.log_count = 0;
+    }
+    if (cb && cb->on_chunk) {
+      thbuf.resize(h->ld);
+      for (int b = 0; b < h->B; ++b) {
+        const TrajG& T = h->htraj[b];
+        size_t off = ((size_t)T.rot_y * h->B + b) * h->ld;
+        CU(kura::launch_unwrap(h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->n, h->fin_theta + (size_t)b * h->ld,
+                               h->stream));
+        CU(cudaMemcpyAsync(thbuf.data(), h->fin_theta + (size_t)b * h->ld, sizeof(float) * h->n,
+                           cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+        if (cb->on_chunk(cb->user, b, T.t, T.h, thbuf.data())) return fail(KURA_ERR_CALLBACK, "on_chunk aborted");
+      }
+    }
+    bool done = true;
+    int errc = 0;
+    for (auto& T : h->htraj) {
+      if (T.status == 0 || T.eval_i < T.eval_end) done = false;
+      if (T.status < 0 && !errc) errc = T.status;
+    }
+    long long after = 0;
+    for (auto& T : h->htraj) after += T.accepted + T.rejected + T.eval_i;
+    if (errc) {
+      const char* m = errc == KURA_ERR_STEP_UNDERFLOW ? "step size underflow" : "non-finite error norm";
+      return fail(errc, m);
+    }
+    if (done) break;
+    stall = (after == before) ? stall + 1 : 0;
+    if (stall > 2) return fail(KURA_ERR_INVALID, "integration made no progress");
+  }
+  long long acc = 0, rej = 0, bars = 0;
+  for (auto& T : h->htraj) { acc += T.accepted; rej += T.rejected; }
+  CU(cudaMemcpy(&bars, h->counters, sizeof(long long), cudaMemcpyDeviceToHost));
+  h->stats.accepted = acc;
+  h->stats.rejected = rej;
+  h->stats.barriers = bars;
+  return KURA_OK;
+}
+
+extern "C" int kura_get_state(kura_handle* h, int32_t traj, float* theta, double* t, double* step) {
+  int rc = check_traj(h, traj);
+  if (rc) return rc;
+  CU(cudaSetDevice(h->cfg.device));
+  const TrajG& T = h->htraj[traj];
+  if (theta) {
+    size_t off = ((size_t)T.rot_y * h->B + traj) * h->ld;
+    float* tmp = h->fin_theta + (size_t)traj * h->ld;
+    CU(kura::launch_unwrap(h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->n, tmp, h->stream));
+    CU(cudaMemcpyAsync(theta, tmp, sizeof(float) * h->n, cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+  }
+  if (t) *t = T.t;
+  if (step) *step = T.h;
+  return KURA_OK;
+}
+
+extern "C" int kura_get_order(kura_handle* h, int32_t traj, float* r, int64_t cap, int64_t* count) {
+  int rc = check_traj(h, traj);
+  if (rc) return rc;
+  const auto& v = h->order[traj];
+  if (count) *count = (int64_t)v.size();
+  if (r) std::memcpy(r, v.data(), sizeof(float) * std::min<size_t>(v.size(), (size_t)std::max<int64_t>(cap, 0)));
+  return KURA_OK;
+}
+
+extern "C" int kura_final_record(kura_handle* h, int32_t traj, float* theta, float* couplings, double* t,
+                                 double* step) {
+  int rc = check_traj(h, traj);
+  if (rc) return rc;
+  if (!h->horizon_set) return fail(KURA_ERR_INVALID, "no run to report");
+  CU(cudaSetDevice(h->cfg.device));
+  rc = launch(h, kura::MODE_FINAL, false);
+  if (rc) return rc;
+  if (theta) CU(cudaMemcpy(theta, h->fin_theta + (size_t)traj * h->ld, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
+  if (couplings)
+    CU(cudaMemcpy(couplings, h->fin_coup + (size_t)traj * 2 * h->ld, sizeof(float) * 2 * h->n, cudaMemcpyDeviceToHost));
+  if (t) *t = h->htraj[traj].t;
+  if (step) *step = h->htraj[traj].h;
+  return KURA_OK;
+}
+
+extern "C" int kura_rhs(kura_handle* h, int32_t traj, const float* theta, float* dtheta, float* couplings) {
+  int rc = check_traj(h, traj);
+  if (rc) return rc;
+  if (!theta) return fail(KURA_ERR_INVALID, "theta is NULL");
+  if (!h->omega_set) return fail(KURA_ERR_INVALID, "frequencies not set");
+  if (h->coupling == KURA_COUPLING_DENSE && !h->adj_set) return fail(KURA_ERR_INVALID, "adjacency not set");
+  CU(cudaSetDevice(h->cfg.device));
+  // the batch is evaluated at its current phases; this trajectory is first set to theta
+  rc = kura_set_state(h, traj, theta, 0.0, 1.0);
+  if (rc) return rc;
+  rc = launch(h, kura::MODE_RHS, false);
+  if (rc) return rc;
+  if (dtheta) CU(cudaMemcpy(dtheta, h->fin_theta + (size_t)traj * h->ld, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
+  if (couplings)
+    CU(cudaMemcpy(couplings, h->fin_coup + (size_t)traj * 2 * h->ld, sizeof(float) * 2 * h->n, cudaMemcpyDeviceToHost));
+  return KURA_OK;
+}
+
+extern "C" int kura_get_stats(kura_handle* h, kura_stats* st) {
+  if (!h || !st) return fail(KURA_ERR_INVALID, "NULL argument");
+  *st = h->stats;
+  return KURA_OK;
+}
+
+extern "C" int kura_volcano_factor(int32_t seed, int64_t n, int32_t k, int8_t* u) {
+  if (n < 1 || k < 0 || !u) return fail(KURA_ERR_INVALID, "bad argument");
+  if (k == 0) return KURA_OK;
+  int words = (k + 31) / 32;
+  uint32_t* d = nullptr;
+  CU(cudaMalloc((void**)&d, sizeof(uint32_t) * (size_t)words * n));
+  cudaError_t e = kura::launch_volcano_words(seed, (int)n, k, words, d, 0);
+  std::vector<uint32_t> hb((size_t)words * n);
+  if (e == cudaSuccess) e = cudaMemcpy(hb.data(), d, sizeof(uint32_t) * hb.size(), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(KURA_ERR_CUDA, cudaGetErrorString(e));
+  for (int m = 0; m < k; ++m)
+    for (int64_t i = 0; i < n; ++i) u[(size_t)m * n + i] = ((hb[(size_t)(m / 32) * n + i] >> (m % 32)) & 1u) ? 1 : -1;
+  return KURA_OK;
+}

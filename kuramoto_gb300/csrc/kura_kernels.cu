@@ -1,0 +1,907 @@
+// kura_kernels.cu -- sm_103a kernels of the Kuramoto DP45 integrator.
+//
+// One persistent cooperative kernel runs the whole adaptive integration
+// (dp45_run, dp45.cu:148-164): the six stage evaluations of each attempt, the
+// error norm, the accept/reject controller, the dense output at every t_eval
+// crossing and the order parameter, with the step size kept on the device.  The
+// host launches it once per run (more often only when an output ring fills).
+//
+// Work split: CTA g owns rows [g*rows, (g+1)*rows) of the network for every
+// trajectory of the batch.  One grid barrier per coupling evaluation exchanges
+// what the other CTAs need:
+//   * dense coupling (kuramoto.cu:110-115): every CTA publishes (cos, sin) of its
+//     rows; after the barrier it streams its rows of A once, computing A*cos and
+//     A*sin together (the reference reads A twice, with two GEMV calls);
+//   * volcano coupling (-A, kuramoto.cu:62-101): every CTA publishes its partial
+//     projections sum_n u_mn (cos, sin); after the barrier each CTA sums the
+//     partials in a fixed order and back-projects for its rows.  The factor bits
+//     come from Philox4x32-10 at stream element m*N+n and are kept in shared memory
+//     for the CTA's rows, so neither A nor the factor is ever stored in HBM.
+// Reductions use fixed orders, so every CTA reaches the same controller
+// decisions and results do not depend on timing.
+//
+// Phases are held as wrapped float pairs (hi in [-pi, pi], lo, winding count),
+// the frequency term omega*h of each stage is added with error-free products,
+// and only the coupling part g = k - omega of each slope is stored.  This keeps
+// the phase accumulation at about double-float accuracy without FP64 arithmetic
+// in the per-oscillator loops (GB300's FP64 rate is a small fraction of FP32).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include "kura.h"
+#include "kura_kernels.cuh"
+
+namespace kura {
+
+// ------------------------------------------------------------------ tableau
+// Dormand-Prince 5(4) weights, nodes, error weights and the 4th-order continuous
+// extension (the same rationals as dp45.cu:6-21).  Row s-1 of A_TAB holds the
+// weights of k_1..k_{s-1} for stage s; row 6 is the 5th-order solution b.
+__constant__ double A_TAB[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {1.0 / 5, 0, 0, 0, 0, 0},
+    {3.0 / 40, 9.0 / 40, 0, 0, 0, 0},
+    {44.0 / 45, -56.0 / 15, 32.0 / 9, 0, 0, 0},
+    {19372.0 / 6561, -25360.0 / 2187, 64448.0 / 6561, -212.0 / 729, 0, 0},
+    {9017.0 / 3168, -355.0 / 33, 46732.0 / 5247, 49.0 / 176, -5103.0 / 18656, 0},
+    {35.0 / 384, 0, 500.0 / 1113, 125.0 / 192, -2187.0 / 6784, 11.0 / 84}};
+__constant__ double C_TAB[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.0};
+__constant__ double E_TAB[7] = {-71.0 / 57600, 0, 71.0 / 16695, -71.0 / 1920, 17253.0 / 339200, -22.0 / 525,
+                                1.0 / 40};
+__constant__ double P_TAB[7][4] = {
+    {1.0, -8048581381.0 / 2820520608, 8663915743.0 / 2820520608, -12715105075.0 / 11282082432},
+    {0, 0, 0, 0},
+    {0, 131558114200.0 / 32700410799, -68118460800.0 / 10900136933, 87487479700.0 / 32700410799},
+    {0, -1754552775.0 / 470086768, 14199869525.0 / 1410260304, -10690763975.0 / 1880347072},
+    {0, 127303824393.0 / 49829197408, -318862633887.0 / 49829197408, 701980252875.0 / 199316789632},
+    {0, -282668133.0 / 205662961, 2019193451.0 / 616988883, -1453857185.0 / 822651844},
+    {0, 40617522.0 / 29380423, -110615467.0 / 29380423, 69997945.0 / 29380423}};
+
+// ------------------------------------------------------------------ float-pair arithmetic
+struct f2 { float hi, lo; };
+__device__ __forceinline__ f2 two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ f2 two_prod(float a, float b) {
+  float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+
+// 2*pi = P2_1 + P2_2 + P2_3 (Cody-Waite split).  With an FMA, hi - k*P2_1 is exact
+// for |k| < 2^24, because both operands are multiples of ulp(P2_1) near the result.
+constexpr double TWO_PI_D = 6.283185307179586476925286766559;
+constexpr float P2_1 = (float)TWO_PI_D;
+constexpr float P2_2 = (float)(TWO_PI_D - (double)P2_1);
+constexpr float P2_3 = (float)(TWO_PI_D - (double)P2_1 - (double)P2_2);
+constexpr float INV_2PI = (float)(1.0 / TWO_PI_D);
+
+__device__ __forceinline__ float reduce_arg(float hi, float lo) {
+  float k = rintf(hi * INV_2PI);
+  float r = __fmaf_rn(-k, P2_1, hi);
+  r = __fmaf_rn(-k, P2_2, r);
+  return __fadd_rn(r, __fmaf_rn(-k, P2_3, lo));
+}
+__device__ __forceinline__ void wrap_phase(float& hi, float& lo, long long& w) {
+  float k = rintf(hi * INV_2PI);
+  if (k != 0.f) {
+    float h2 = __fmaf_rn(-k, P2_1, hi);
+    float l2 = __fadd_rn(lo, __fmaf_rn(-k, P2_2, __fmul_rn(-k, P2_3)));
+    f2 s = two_sum(h2, l2);
+    hi = s.hi;
+    lo = s.lo;
+    w += (long long)k;
+  }
+}
+
+// ------------------------------------------------------------------ Philox4x32-10
+// Salmon et al. (SC'11).  Stream element q: block q/4 (128-bit counter), word q%4,
+// key = the seed widened like an int passed to curand_init (kuramoto.cu:57-60).
+__device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+  }
+  return c;
+}
+__device__ __forceinline__ uint32_t stream_word(int seed, unsigned long long q) {
+  unsigned long long s = (unsigned long long)(long long)seed;
+  uint4 o = philox10(make_uint4((uint32_t)(q >> 2), (uint32_t)(q >> 34), 0u, 0u), (uint32_t)s, (uint32_t)(s >> 32));
+  uint32_t sel = (uint32_t)(q & 3);
+  return sel == 0 ? o.x : sel == 1 ? o.y : sel == 2 ? o.z : o.w;
+}
+
+// ------------------------------------------------------------------ memory helpers
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// streamed read of the adjacency: no L1 allocation, default L2 policy (a small A stays L2-resident)
+__device__ __forceinline__ float4 ld_stream4(const float* p) {
+  float4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p));
+  return v;
+}
+
+// ------------------------------------------------------------------ per-evaluation source
+// What one coupling evaluation integrates for one trajectory:
+//   theta = phase[base] + omega*(m_hi + m_lo) + sum_j W[j] * g[slot[j]]
+struct SrcB {
+  float W[7];
+  float E[7];      // error weights h*e_j (error phase)
+  float m_hi, m_lo;
+  int slot[7];     // physical g slot of logical k_1..k_7
+  int base;        // physical phase buffer
+  int gout;        // g slot receiving c*(sin*Fc - cos*Fs), -1: none
+  int active;
+  int store_y7;    // keep the stage value (the candidate y) in buffer base^1
+  int rec;         // output record (r always; theta / couplings by dense level)
+  int oslot, oidx;
+  int nW;
+};
+
+__device__ __forceinline__ int slot_k1(int rot_g) { return rot_g ? 6 : 0; }
+__device__ __forceinline__ int slot_k7(int rot_g) { return rot_g ? 0 : 6; }
+
+__host__ __device__ constexpr int pw_of(int coup, int kmax) { return coup == KURA_COUPLING_VOLCANO ? 2 * kmax + 2 : 2; }
+__host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
+
+// shared-memory layout (bytes), also used by the host to size the launch
+__host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int rows, int* off, int* total) {
+  int pw = pw_of(coup, kmax);
+  int o = 0;
+  off[0] = o; o += align16(bmax * (int)sizeof(TrajG));
+  off[1] = o; o += align16(bmax * (int)sizeof(SrcB));
+  off[2] = o; o += align16(KW * bmax * pw * 4);          // red
+  off[3] = o; o += align16(bmax * pw * 4);               // rsum
+  int sl = KT > bmax * pw ? KT : bmax * pw;
+  off[4] = o; o += align16(sl * 4);                      // slice
+  off[5] = o; o += align16(16 * 4);                      // flags
+  off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
+  off[7] = o; o += align16(coup == KURA_COUPLING_DENSE ? bmax * CT * 8 : 0); // x tile
+  off[8] = o; o += align16(bmax * 2 * kmax * 4);         // f3 (volcano)
+  *total = o;
+}
+
+template <int COUP, int BMAX, int KMAX>
+struct Engine {
+  static constexpr int PW = pw_of(COUP, KMAX);
+  static constexpr int RG = BMAX == 1 ? 4 : (BMAX == 2 ? 2 : 1);
+
+  const KParams& p;
+  TrajG* tr;
+  SrcB* sb;
+  float* red;
+  float* rsum;
+  float* slice;
+  int* flag;
+  uint32_t* ubits;
+  float2* xt;
+  float* f3;
+  int G, gi, tid, lane, warp, r0, r1, B;
+  unsigned target;
+  int nbar, xpar;
+
+  __device__ Engine(const KParams& pp, unsigned char* smem) : p(pp) {
+    int off[9], total;
+    smem_layout(COUP, BMAX, KMAX, pp.rows, off, &total);
+    tr = (TrajG*)(smem + off[0]);
+    sb = (SrcB*)(smem + off[1]);
+    red = (float*)(smem + off[2]);
+    rsum = (float*)(smem + off[3]);
+    slice = (float*)(smem + off[4]);
+    flag = (int*)(smem + off[5]);
+    ubits = (uint32_t*)(smem + off[6]);
+    xt = (float2*)(smem + off[7]);
+    f3 = (float*)(smem + off[8]);
+    G = gridDim.x;
+    gi = blockIdx.x;
+    tid = threadIdx.x;
+    lane = tid & 31;
+    warp = tid >> 5;
+    r0 = min(p.n, gi * p.rows);
+    r1 = min(p.n, r0 + p.rows);
+    B = p.batch;
+    target = 0;
+    nbar = 0;
+    xpar = 0;
+  }
+
+  // Grid barrier with a time limit.  Returns false (on every thread) when the
+  // launch is being abandoned: this CTA timed out or another CTA flagged an error.
+  __device__ bool grid_sync() {
+    __syncthreads();
+    target += (unsigned)G;
+    if (tid == 0) {
+      __threadfence();
+      red_release_add(p.bar, 1u);
+      unsigned long long t0 = global_ns();
+      int abort = 0;
+      unsigned spins = 0;
+      while (true) {
+        unsigned v = ld_acquire_u32(p.bar);
+        if ((int)(v - (target + p.bar_extra)) >= 0) break;
+        if (*(volatile int*)p.err != 0) { abort = 1; break; }
+        if ((++spins & 63u) == 0 && global_ns() - t0 > p.timeout_ns) {
+          atomicCAS(p.err, 0, KURA_ERR_BARRIER_TIMEOUT);
+          abort = 1;
+          break;
+        }
+      }
+      __threadfence();
+      flag[0] = abort;
+    }
+    __syncthreads();
+    nbar++;
+    return flag[0] == 0;
+  }
+
+  __device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+  }
+
+  // red[warp][b][*] -> part[par][gi][b][*]
+  __device__ void publish_partials(int npw) {
+    __syncthreads();
+    int par = nbar & 1;
+    for (int v = tid; v < B * npw; v += KT) {
+      int b = v / npw, w = v % npw;
+      float s = 0.f;
+      for (int q = 0; q < KW; ++q) s += red[(q * BMAX + b) * PW + w];
+      p.part[((size_t)(par * G + gi) * B + b) * PW_MAX + w] = s;
+    }
+  }
+  // part[par][*][b][w] summed over CTAs in a fixed order -> rsum[b*PW + w]
+  __device__ void gather_partials(int npw) {
+    int par = (nbar - 1) & 1;  // the parity published before the barrier just passed
+    int NV = B * npw;
+    int S = KT / NV;
+    if (S < 1) S = 1;
+    if (S > G) S = G;
+    for (int t = tid; t < S * NV; t += KT) {
+      int v = t % NV, sl = t / NV;
+      int b = v / npw, w = v % npw;
+      int g0 = (int)((long long)sl * G / S), g1 = (int)((long long)(sl + 1) * G / S);
+      float s = 0.f;
+      for (int g = g0; g < g1; ++g) s += __ldcg(&p.part[((size_t)(par * G + g) * B + b) * PW_MAX + w]);
+      slice[sl * NV + v] = s;
+    }
+    __syncthreads();
+    for (int v = tid; v < NV; v += KT) {
+      float s = 0.f;
+      for (int sl = 0; sl < S; ++sl) s += slice[sl * NV + v];
+      rsum[(v / npw) * PW + (v % npw)] = s;
+    }
+    __syncthreads();
+  }
+
+  // ---- epilogue of one row: slope, couplings, RHS output
+  __device__ __forceinline__ void epilogue(int b, int i, float Fc, float Fs, float cs, float sn) {
+    const SrcB& s = sb[b];
+    float gval = tr[b].c1 * (sn * Fc - cs * Fs);
+    if (s.gout >= 0) p.g[((size_t)s.gout * B + b) * p.ld + i] = gval;
+    if (s.rec) {
+      if (p.mode == MODE_INTEGRATE) {
+        if (p.dense_level >= 2) {
+          float* dst = p.out_coup + ((size_t)b * p.ring + s.oslot) * 2 * p.ld;
+          dst[2 * i] = Fc;
+          dst[2 * i + 1] = Fs;
+        }
+      } else {
+        float* dst = p.fin_coup + (size_t)b * 2 * p.ld;
+        dst[2 * i] = Fc;
+        dst[2 * i + 1] = Fs;
+        if (p.mode == MODE_RHS) p.fin_theta[(size_t)b * p.ld + i] = p.omega[i] + gval;
+      }
+    }
+  }
+
+  // ---- one coupling evaluation for every active trajectory (one grid barrier)
+  __device__ bool coupling_eval(bool want_r) {
+    const int n = p.n, ld = p.ld;
+    const bool need_part = (COUP == KURA_COUPLING_VOLCANO) || want_r;
+    // phase A: stage value, sincos, exchange data and partial sums
+    for (int b = 0; b < B; ++b) {
+      const SrcB& s = sb[b];
+      float acc[PW];
+#pragma unroll
+      for (int v = 0; v < PW; ++v) acc[v] = 0.f;
+      if (s.active) {
+        const float* hiB = p.ph_hi + ((size_t)s.base * B + b) * ld;
+        const float* loB = p.ph_lo + ((size_t)s.base * B + b) * ld;
+        for (int i = r0 + tid; i < r1; i += KT) {
+          float om = p.omega[i];
+          float gsum = 0.f;
+          for (int j = 0; j < s.nW; ++j) gsum = __fmaf_rn(s.W[j], p.g[((size_t)s.slot[j] * B + b) * ld + i], gsum);
+          f2 pr = two_prod(om, s.m_hi);
+          float pl = om * s.m_lo;
+          f2 s1 = two_sum(hiB[i], pr.hi);
+          f2 s2 = two_sum(s1.hi, gsum);
+          float lo = loB[i] + ((s1.lo + s2.lo) + (pr.lo + pl));
+          float arg = reduce_arg(s2.hi, lo);
+          float sn, cs;
+          sincosf(arg, &sn, &cs);
+          p.xbuf[((size_t)xpar * B + b) * ld + i] = make_float2(cs, sn);
+          if (s.store_y7 || (s.rec && p.dense_level >= 1 && p.mode == MODE_INTEGRATE) || (s.rec && p.mode == MODE_FINAL)) {
+            f2 y = two_sum(s2.hi, lo);
+            long long w = p.ph_w[((size_t)s.base * B + b) * ld + i];
+            if (s.store_y7) {
+              float hi7 = y.hi, lo7 = y.lo;
+              long long w7 = w;
+              wrap_phase(hi7, lo7, w7);
+              size_t o = ((size_t)(s.base ^ 1) * B + b) * ld + i;
+              p.ph_hi[o] = hi7;
+              p.ph_lo[o] = lo7;
+              p.ph_w[o] = w7;
+            } else {
+              double th = (double)w * TWO_PI_D + (double)y.hi + (double)y.lo;
+              if (p.mode == MODE_INTEGRATE)
+                p.out_theta[((size_t)b * p.ring + s.oslot) * ld + i] = (float)th;
+              else
+                p.fin_theta[(size_t)b * ld + i] = (float)th;
+            }
+          }
+          if (COUP == KURA_COUPLING_VOLCANO) {
+            uint32_t u = ubits[i - r0];
+#pragma unroll
+            for (int m = 0; m < KMAX; ++m) {
+              if (m < p.k) {
+                float sg = ((u >> m) & 1u) ? 1.f : -1.f;
+                acc[2 * m] = __fmaf_rn(sg, cs, acc[2 * m]);
+                acc[2 * m + 1] = __fmaf_rn(sg, sn, acc[2 * m + 1]);
+              }
+            }
+          }
+          if (want_r) {
+            acc[PW - 2] += cs;
+            acc[PW - 1] += sn;
+          }
+        }
+      }
+      if (need_part) {
+#pragma unroll
+        for (int v = 0; v < PW; ++v) {
+          float t = warp_sum(acc[v]);
+          if (lane == 0) red[(warp * BMAX + b) * PW + v] = t;
+        }
+      }
+    }
+    if (need_part) publish_partials(PW);
+    if (!grid_sync()) return false;
+    if (need_part) gather_partials(PW);
+
+    // phase C: couplings for the CTA's rows
+    if (COUP == KURA_COUPLING_VOLCANO) {
+      // f3[b][2m] = (-1)^m / N * sum_n u_mn cos_n (m1, kuramoto.cu:62-81)
+      for (int v = tid; v < B * 2 * KMAX; v += KT) {
+        int b = v / (2 * KMAX), w = v % (2 * KMAX);
+        int m = w >> 1;
+        float sgn = (m & 1) ? -1.f : 1.f;
+        f3[v] = (m < p.k) ? (sgn * rsum[b * PW + w]) / (float)n : 0.f;
+      }
+      __syncthreads();
+      for (int b = 0; b < B; ++b) {
+        if (!sb[b].active) continue;
+        const float2* xb = p.xbuf + ((size_t)xpar * B + b) * ld;
+        const float* fb = f3 + b * 2 * KMAX;
+        for (int i = r0 + tid; i < r1; i += KT) {
+          uint32_t u = ubits[i - r0];
+          float Fc = 0.f, Fs = 0.f;
+          // m2 (kuramoto.cu:83-101): F_n = sum_m u_mn f3_m, sequential in m
+#pragma unroll
+          for (int m = 0; m < KMAX; ++m) {
+            if (m < p.k) {
+              bool pos = (u >> m) & 1u;
+              Fc += pos ? fb[2 * m] : -fb[2 * m];
+              Fs += pos ? fb[2 * m + 1] : -fb[2 * m + 1];
+            }
+          }
+          float2 x = xb[i];
+          epilogue(b, i, Fc, Fs, x.x, x.y);
+        }
+      }
+    } else {
+      dense_matvec();
+    }
+    if (want_r && gi == 0 && tid == 0) {
+      for (int b = 0; b < B; ++b) {
+        const SrcB& s = sb[b];
+        if (!s.active || !s.rec || p.mode != MODE_INTEGRATE) continue;
+        float X = rsum[b * PW + PW - 2], Y = rsum[b * PW + PW - 1];
+        float xn = X / (float)n, yn = Y / (float)n;
+        p.out_r[(size_t)b * p.ring + s.oslot] = sqrtf(xn * xn + yn * yn);
+        p.out_idx[(size_t)b * p.ring + s.oslot] = s.oidx;
+      }
+    }
+    xpar ^= 1;
+    __syncthreads();
+    return true;
+  }
+
+  // A (rows r0..r1 of this CTA) times the (cos, sin) of every trajectory.  x is
+  // staged in shared memory one column tile at a time; each warp keeps RG rows in
+  // flight, each lane reading 16-byte chunks of them.
+  __device__ void dense_matvec() {
+    const int ld = p.ld;
+    const int rows_per_pass = KW * RG;
+    for (int pr0 = r0; pr0 < r1; pr0 += rows_per_pass) {
+      float acc[RG][BMAX][2];
+#pragma unroll
+      for (int q = 0; q < RG; ++q)
+#pragma unroll
+        for (int b = 0; b < BMAX; ++b) acc[q][b][0] = acc[q][b][1] = 0.f;
+      const int row0 = pr0 + warp * RG;
+      for (int c0 = 0; c0 < ld; c0 += CT) {
+        __syncthreads();
+        const int cw = min(CT, ld - c0);
+        for (int t = tid; t < B * CT; t += KT) {
+          int b = t / CT, c = t - b * CT;
+          xt[b * CT + c] = (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        for (int cc = lane * 4; cc < cw; cc += 128) {
+          float4 a[RG];
+#pragma unroll
+          for (int q = 0; q < RG; ++q) {
+            int row = row0 + q;
+            a[q] = (row < r1) ? ld_stream4(p.adj + (size_t)row * ld + c0 + cc) : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+#pragma unroll
+          for (int b = 0; b < BMAX; ++b) {
+            if (b < B) {
+              const float4* xp = reinterpret_cast<const float4*>(xt + b * CT + cc);
+              float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
+#pragma unroll
+              for (int q = 0; q < RG; ++q) {
+                acc[q][b][0] += a[q].x * x01.x + a[q].y * x01.z + a[q].z * x23.x + a[q].w * x23.z;
+                acc[q][b][1] += a[q].x * x01.y + a[q].y * x01.w + a[q].z * x23.y + a[q].w * x23.w;
+              }
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RG; ++q)
+#pragma unroll
+        for (int b = 0; b < BMAX; ++b) {
+          acc[q][b][0] = warp_sum(acc[q][b][0]);
+          acc[q][b][1] = warp_sum(acc[q][b][1]);
+        }
+      // lane q*BMAX+b finishes row row0+q of trajectory b
+#pragma unroll
+      for (int q = 0; q < RG; ++q)
+#pragma unroll
+        for (int b = 0; b < BMAX; ++b) {
+          int row = row0 + q;
+          if (lane == q * BMAX + b && b < B && row < r1 && sb[b].active) {
+            float2 x = __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + row]);
+            epilogue(b, row, acc[q][b][0], acc[q][b][1], x.x, x.y);
+          }
+        }
+    }
+  }
+
+  // ---- error norm of the attempt (dp45.cu:79-84, 116-119); sum of squares -> rsum[b*PW]
+  __device__ bool error_phase() {
+    const int ld = p.ld;
+    for (int b = 0; b < B; ++b) {
+      const SrcB& s = sb[b];
+      float acc = 0.f;
+      if (s.active) {
+        const size_t yb = ((size_t)s.base * B + b) * ld, y7b = ((size_t)(s.base ^ 1) * B + b) * ld;
+        for (int i = r0 + tid; i < r1; i += KT) {
+          float e = 0.f;
+#pragma unroll
+          for (int j = 0; j < 7; ++j) e = __fmaf_rn(s.E[j], p.g[((size_t)s.slot[j] * B + b) * ld + i], e);
+          float tol = (float)p.atol;
+          if (p.rtol != 0.0) {
+            float a0 = fabsf(__fmaf_rn((float)p.ph_w[yb + i], P2_1, p.ph_hi[yb + i]));
+            float a1 = fabsf(__fmaf_rn((float)p.ph_w[y7b + i], P2_1, p.ph_hi[y7b + i]));
+            tol = (float)p.atol + (float)p.rtol * fmaxf(a0, a1);
+          }
+          float ye = e / tol;
+          acc = __fmaf_rn(ye, ye, acc);
+        }
+      }
+      float t = warp_sum(acc);
+      if (lane == 0) {
+        red[(warp * BMAX + b) * PW] = t;
+#pragma unroll
+        for (int v = 1; v < PW; ++v) red[(warp * BMAX + b) * PW + v] = 0.f;
+      }
+    }
+    publish_partials(1);
+    if (!grid_sync()) return false;
+    gather_partials(1);
+    return true;
+  }
+
+  // ---- per-trajectory sources (thread 0 only)
+  __device__ void set_stage_src(int b, int s, float hf) {
+    SrcB& S = sb[b];
+    const TrajG& T = tr[b];
+    for (int j = 0; j < 7; ++j) S.W[j] = 0.f;
+    for (int j = 0; j < s - 1; ++j) S.W[j] = (float)((double)hf * A_TAB[s - 1][j]);
+    S.nW = s - 1;
+    double mh = C_TAB[s - 1] * (double)hf;
+    S.m_hi = (float)mh;
+    S.m_lo = (float)(mh - (double)S.m_hi);
+    S.slot[0] = slot_k1(T.rot_g);
+    for (int j = 1; j < 6; ++j) S.slot[j] = j;
+    S.slot[6] = slot_k7(T.rot_g);
+    S.base = T.rot_y;
+    S.gout = (s < 7) ? s - 1 : slot_k7(T.rot_g);
+    S.store_y7 = (s == 7);
+    S.rec = 0;
+    S.oslot = -1;
+    S.oidx = 0;
+    for (int j = 0; j < 7; ++j) S.E[j] = (float)((double)hf * E_TAB[j]);
+  }
+  // dense output at t_eval from the last accepted step (interpolate, dp45.cu:70-76).
+  // k1_slot / k7_slot choose the physical slopes; the end-of-run record passes the
+  // slot of k7 for both, as the reference's FSAL copy leaves it (dp45.cu:160).
+  __device__ void set_eval_src(int b, double te, int k1_slot, int k7_slot) {
+    SrcB& S = sb[b];
+    const TrajG& T = tr[b];
+    double hs = T.t - T.t_last;
+    double dl = te - T.t_last;
+    double x = dl / hs;
+    for (int j = 0; j < 7; ++j) {
+      double c = P_TAB[j][0] * x + P_TAB[j][1] * x * x + P_TAB[j][2] * x * x * x + P_TAB[j][3] * x * x * x * x;
+      S.W[j] = (float)(hs * c);
+    }
+    S.nW = 7;
+    S.m_hi = (float)dl;
+    S.m_lo = (float)(dl - (double)S.m_hi);
+    S.slot[0] = k1_slot;
+    for (int j = 1; j < 6; ++j) S.slot[j] = j;
+    S.slot[6] = k7_slot;
+    S.base = T.rot_y ^ 1;
+    S.gout = -1;
+    S.store_y7 = 0;
+    S.rec = 1;
+  }
+  __device__ void set_y_src(int b) {
+    SrcB& S = sb[b];
+    const TrajG& T = tr[b];
+    for (int j = 0; j < 7; ++j) S.W[j] = 0.f;
+    S.nW = 0;
+    S.m_hi = S.m_lo = 0.f;
+    for (int j = 0; j < 7; ++j) S.slot[j] = j;
+    S.base = T.rot_y;
+    S.gout = -1;
+    S.store_y7 = 0;
+    S.rec = 0;
+    S.oslot = -1;
+    S.oidx = -1;
+  }
+
+  __device__ void write_back() {
+    if (gi == 0 && tid < B) p.traj[tid] = tr[tid];
+    if (gi == 0 && tid == 0) atomicAdd((unsigned long long*)p.counters, (unsigned long long)nbar);
+  }
+
+  // ---- the whole launch
+  __device__ void run() {
+    if (tid < B) tr[tid] = p.traj[tid];
+    if (COUP == KURA_COUPLING_VOLCANO) {
+      for (int lr = tid; lr < r1 - r0; lr += KT) {
+        int i = r0 + lr;
+        uint32_t w = 0;
+        for (int m = 0; m < p.k; ++m)
+          w |= (stream_word(p.seed, (unsigned long long)m * (unsigned long long)p.n + (unsigned long long)i) & 1u) << m;
+        ubits[lr] = w;
+      }
+    }
+    __syncthreads();
+
+    if (p.mode == MODE_FINAL || p.mode == MODE_RHS) {
+      if (tid == 0) {
+        for (int b = 0; b < B; ++b) {
+          const TrajG& T = tr[b];
+          set_y_src(b);
+          SrcB& S = sb[b];
+          S.active = 1;
+          S.rec = 1;
+          if (p.mode == MODE_FINAL && p.n_eval > 0 && T.accepted > 0) {
+            int ks = slot_k1(T.rot_g);  // after the last FSAL swap this slot holds k7
+            set_eval_src(b, (double)p.t_eval[p.n_eval - 1], ks, ks);
+            S.active = 1;
+          }
+        }
+      }
+      __syncthreads();
+      if (!coupling_eval(false)) return;
+      write_back();
+      return;
+    }
+
+    // first slope of the run (dp45.cu:151) and the record at t0 (kuramoto.cu:587-626)
+    if (tid == 0) {
+      int any = 0;
+      for (int b = 0; b < B; ++b) {
+        TrajG& T = tr[b];
+        set_y_src(b);
+        SrcB& S = sb[b];
+        S.active = (T.status == 0 && T.need_k1);
+        if (S.active) {
+          S.gout = slot_k1(T.rot_g);
+          if (T.need_init && T.out_count < p.ring) {
+            S.rec = 1;
+            S.oslot = T.out_count;
+            S.oidx = -1;
+          }
+          any = 1;
+        }
+      }
+      flag[1] = any;
+    }
+    __syncthreads();
+    if (flag[1]) {
+      bool want_r = false;
+      for (int b = 0; b < B; ++b) want_r |= (sb[b].active && sb[b].rec);
+      if (!coupling_eval(want_r)) return;
+      if (tid == 0) {
+        for (int b = 0; b < B; ++b) {
+          if (!sb[b].active) continue;
+          tr[b].need_k1 = 0;
+          if (sb[b].rec) { tr[b].need_init = 0; tr[b].out_count++; }
+        }
+      }
+      __syncthreads();
+    }
+
+    long long attempts = 0;
+    while (true) {
+      if (tid == 0) {
+        int todo_out = 0, todo_step = 0, stop = 0;
+        for (int b = 0; b < B; ++b) {
+          TrajG& T = tr[b];
+          if (T.status != 0) continue;
+          if (T.eval_i < T.eval_end) {
+            if (T.out_count < p.ring) todo_out = 1; else stop = 1;
+            continue;
+          }
+          if (!(T.t < T.t1)) { T.status = 1; continue; }
+          if (p.log_cap > 0 && T.log_count >= p.log_cap) { stop = 1; continue; }
+          todo_step = 1;
+        }
+        if (p.max_attempts >= 0 && attempts >= p.max_attempts) stop = 1;
+        flag[1] = todo_out;
+        flag[2] = todo_step;
+        flag[3] = stop;
+        if (todo_out) {
+          for (int b = 0; b < B; ++b) {
+            TrajG& T = tr[b];
+            SrcB& S = sb[b];
+            S.active = (T.status == 0 && T.eval_i < T.eval_end && T.out_count < p.ring);
+            if (S.active) {
+              // after the accept, k1 of the step sits in the k7 slot and vice versa
+              set_eval_src(b, (double)p.t_eval[T.eval_i], slot_k7(T.rot_g), slot_k1(T.rot_g));
+              S.oslot = T.out_count;
+              S.oidx = T.eval_i;
+            }
+          }
+        }
+      }
+      __syncthreads();
+      if (flag[1]) {
+        if (!coupling_eval(true)) return;
+        if (tid == 0) {
+          for (int b = 0; b < B; ++b)
+            if (sb[b].active) { tr[b].eval_i++; tr[b].out_count++; }
+        }
+        __syncthreads();
+        continue;
+      }
+      if (flag[3] || !flag[2]) break;
+
+      // ---- one attempt of every stepping trajectory (dp45_step, dp45.cu:87-141)
+      if (tid == 0) {
+        for (int b = 0; b < B; ++b) {
+          const TrajG& T = tr[b];
+          sb[b].active = (T.status == 0 && T.eval_i >= T.eval_end && T.t < T.t1 &&
+                          !(p.log_cap > 0 && T.log_count >= p.log_cap));
+        }
+      }
+      __syncthreads();
+      for (int s = 2; s <= 7; ++s) {
+        if (tid == 0) {
+          for (int b = 0; b < B; ++b) {
+            int act = sb[b].active;
+            set_stage_src(b, s, (float)tr[b].h);
+            sb[b].active = act;
+          }
+        }
+        __syncthreads();
+        if (!coupling_eval(false)) return;
+      }
+      if (!p.fixed) {
+        if (!error_phase()) return;
+      }
+      if (tid == 0) {
+        for (int b = 0; b < B; ++b) {
+          if (!sb[b].active) continue;
+          TrajG& T = tr[b];
+          float hf = (float)T.h;
+          bool accept = true;
+          double factor = 1.0;
+          if (!p.fixed) {
+            double norm = sqrt((double)rsum[b * PW]) / sqrt((double)p.n);
+            if (!isfinite(norm)) { T.status = KURA_ERR_NONFINITE; continue; }
+            factor = 0.9 * pow(norm, -0.2);
+            accept = norm < 1.0;
+          }
+          if (accept) {
+            T.t_last = T.t;
+            T.t = T.t + (double)hf;
+            T.rot_y ^= 1;
+            T.rot_g ^= 1;
+            T.accepted++;
+            if (!p.fixed) T.h = (double)hf * fmin(factor, 10.0);
+            int e = T.eval_i;
+            while (e < p.n_eval && T.t >= (double)p.t_eval[e]) e++;
+            T.eval_end = e;
+            if (p.log_cap > 0) {
+              p.log_t[(size_t)b * p.log_cap + T.log_count] = T.t;
+              p.log_h[(size_t)b * p.log_cap + T.log_count] = T.h;
+            }
+            T.log_count++;
+          } else {
+            T.rejected++;
+            if (factor < 1.0) T.h = (double)hf * fmax(factor, 0.2);
+            if (!(T.h >= 1e-14 * fmax(1.0, fabs(T.t)))) T.status = KURA_ERR_STEP_UNDERFLOW;
+          }
+        }
+      }
+      __syncthreads();
+      attempts++;
+    }
+    write_back();
+  }
+};
+
+template <int COUP, int BMAX, int KMAX>
+__global__ void __launch_bounds__(KT, 1) k_persistent(const KParams p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Engine<COUP, BMAX, KMAX> e(p, smem);
+  e.run();
+}
+
+template <int COUP, int BMAX, int KMAX>
+static const void* kernel_ptr() {
+  return (const void*)&k_persistent<COUP, BMAX, KMAX>;
+}
+
+static const void* pick_kernel(int coupling, int bmax, int kmax) {
+  if (coupling == KURA_COUPLING_DENSE) {
+    if (bmax == 1) return kernel_ptr<KURA_COUPLING_DENSE, 1, 1>();
+    if (bmax == 8) return kernel_ptr<KURA_COUPLING_DENSE, 8, 1>();
+  } else {
+    if (bmax == 1 && kmax == 8) return kernel_ptr<KURA_COUPLING_VOLCANO, 1, 8>();
+    if (bmax == 8 && kmax == 8) return kernel_ptr<KURA_COUPLING_VOLCANO, 8, 8>();
+    if (bmax == 1 && kmax == 32) return kernel_ptr<KURA_COUPLING_VOLCANO, 1, 32>();
+    if (bmax == 8 && kmax == 32) return kernel_ptr<KURA_COUPLING_VOLCANO, 8, 32>();
+  }
+  return nullptr;
+}
+
+cudaError_t persistent_config(int coupling, int bmax, int kmax, size_t* smem_bytes, int* blocks_per_sm,
+                              int rows_per_cta) {
+  const void* f = pick_kernel(coupling, bmax, kmax);
+  if (!f) return cudaErrorInvalidValue;
+  int off[9], total;
+  smem_layout(coupling, bmax, coupling == KURA_COUPLING_DENSE ? 1 : kmax, rows_per_cta, off, &total);
+  *smem_bytes = (size_t)total;
+  cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, total);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, KT, (size_t)total);
+}
+
+cudaError_t launch_persistent(const KParams& p, int grid, int bmax, int kmax, size_t smem, cudaStream_t st) {
+  const void* f = pick_kernel(p.coupling, bmax, kmax);
+  if (!f) return cudaErrorInvalidValue;
+  KParams copy = p;
+  void* args[] = {&copy};
+  return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(KT), args, smem, st);
+}
+
+// ------------------------------------------------------------------ small kernels
+// theta (unwrapped float) -> wrapped (hi, lo, winding)
+__global__ void k_init_state(const float* __restrict__ theta, int n, float* hi, float* lo, long long* w) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    double t = (double)theta[i];
+    double k = rint(t / TWO_PI_D);
+    double r = t - k * TWO_PI_D;
+    float h = (float)r;
+    hi[i] = h;
+    lo[i] = (float)(r - (double)h);
+    w[i] = (long long)k;
+  }
+}
+__global__ void k_unwrap(const float* hi, const float* lo, const long long* w, int n, float* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)((double)w[i] * TWO_PI_D + (double)hi[i] + (double)lo[i]);
+}
+cudaError_t launch_init_state(const float* theta, int n, int ld, float* hi, float* lo, long long* w,
+                              cudaStream_t st) {
+  (void)ld;
+  if (n <= 0) return cudaSuccess;
+  k_init_state<<<(n + 255) / 256, 256, 0, st>>>(theta, n, hi, lo, w);
+  return cudaGetLastError();
+}
+cudaError_t launch_unwrap(const float* hi, const float* lo, const long long* w, int n, float* out,
+                          cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_unwrap<<<(n + 255) / 256, 256, 0, st>>>(hi, lo, w, n, out);
+  return cudaGetLastError();
+}
+
+// factor bits packed per oscillator: bits[wd*n + i] bit (m - 32*wd) = low bit of element m*n+i
+__global__ void k_volcano_words(int seed, int n, int k, int words, uint32_t* bits) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * words) return;
+  int i = (int)(t % n), wd = (int)(t / n);
+  uint32_t w = 0;
+  int m0 = 32 * wd, m1 = min(k, m0 + 32);
+  for (int m = m0; m < m1; ++m)
+    w |= (stream_word(seed, (unsigned long long)m * (unsigned long long)n + (unsigned long long)i) & 1u) << (m - m0);
+  bits[(size_t)wd * n + i] = w;
+}
+cudaError_t launch_volcano_words(int seed, int n, int k, int words, uint32_t* bits, cudaStream_t st) {
+  long long tot = (long long)n * words;
+  if (tot <= 0) return cudaSuccess;
+  k_volcano_words<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(seed, n, k, words, bits);
+  return cudaGetLastError();
+}
+
+// N*A_ij = sum_m (-1)^m u_mi u_mj = (#even m) - (#odd m) - 2*popc(even disagreements) + 2*popc(odd ones);
+// the entry is that integer times fl(1/N), rounded once (kuramoto.cu:137-157 forms it by a GEMM).
+__global__ void k_volcano_adjacency(const uint32_t* __restrict__ bits, int n, int k, int words, int ld,
+                                    float* __restrict__ adj) {
+  const float invn = 1.0f / (float)n;
+  for (int i = blockIdx.y; i < n; i += gridDim.y)
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ld; j += gridDim.x * blockDim.x) {
+    float v = 0.f;
+    if (j < n) {
+      int kk = 0;
+      for (int wd = 0; wd < words; ++wd) {
+        int m0 = 32 * wd, cnt = min(32, k - m0);
+        uint32_t valid = cnt >= 32 ? 0xffffffffu : ((1u << cnt) - 1u);
+        uint32_t even = 0x55555555u & valid, odd = 0xAAAAAAAAu & valid;  // m0 is even
+        uint32_t dis = bits[(size_t)wd * n + i] ^ bits[(size_t)wd * n + j];
+        kk += __popc(even) - __popc(odd) - 2 * __popc(dis & even) + 2 * __popc(dis & odd);
+      }
+      v = __fmul_rn((float)kk, invn);
+    }
+    adj[(size_t)i * ld + j] = v;
+  }
+}
+cudaError_t launch_volcano_adjacency(const uint32_t* bits, int n, int k, int words, int ld, float* adj,
+                                     cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  dim3 grid((unsigned)min((ld + 255) / 256, 64), (unsigned)min(n, 65535));
+  k_volcano_adjacency<<<grid, 256, 0, st>>>(bits, n, k, words, ld, adj);
+  return cudaGetLastError();
+}
+
+}  // namespace kura

@@ -1,0 +1,78 @@
+// kura_kernels.cuh -- device-side data structures shared by the kernels and the
+// C ABI implementation of libkura.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kura {
+
+constexpr int KT = 512;       // threads per CTA of the persistent integrator
+constexpr int KW = KT / 32;   // warps per CTA
+constexpr int CT = 1024;      // columns per staged x tile of the dense coupling
+constexpr int PW_MAX = 2 * 32 + 2;  // partial sums per trajectory and CTA: 2K projections + (sum cos, sum sin)
+
+// Per-trajectory scalars.  Every CTA keeps an identical copy in shared memory
+// and takes identical decisions from identical data; CTA 0 writes it back.
+struct TrajG {
+  double t, h, t_last, t1;
+  long long accepted, rejected;
+  int status;      // 0 running, 1 finished, < 0 a KURA_ERR_* code
+  int eval_i;      // next output index into t_eval
+  int eval_end;    // one past the last output owed by the last accepted step
+  int rot_y;       // physical phase buffer holding y (the other holds ylast / y7)
+  int rot_g;       // FSAL: 0 -> k1 in g slot 0 and k7 in slot 6; 1 -> swapped
+  int need_k1;     // the first RHS of a run is still to be evaluated
+  int need_init;   // fresh start: record r(theta0) (and theta0, couplings) first
+  int out_count;   // output records written in this launch
+  int log_count;   // accepted steps logged in this launch
+  float c1;        // coupling constant
+  int pad[2];
+};
+
+struct KParams {
+  int n, ld, batch, k, coupling, dense_level, fixed, rows, seed, mode;
+  const float* omega;  // [ld]
+  const float* adj;    // [n][ld] dense coupling
+  float* ph_hi;        // [2][B][ld] wrapped phase, high part
+  float* ph_lo;        // [2][B][ld] low part
+  long long* ph_w;     // [2][B][ld] 2*pi windings
+  float* g;            // [7][B][ld] coupling part of the stage slopes k_j - omega
+  float2* xbuf;        // [2][B][ld] (cos, sin) exchanged between CTAs
+  float* part;         // [2][grid][B][PW_MAX] per-CTA partial sums
+  unsigned* bar;       // grid barrier arrival counter (zeroed before each launch)
+  int* err;            // launch-wide abort code
+  TrajG* traj;         // [B]
+  const float* t_eval; // output grid
+  int n_eval;
+  double atol, rtol, dt;
+  float* out_r;        // [B][ring] order parameter records
+  int* out_idx;        // [B][ring] output index (-1: the record at t0)
+  float* out_theta;    // [B][ring][ld] unwrapped phases (dense_level >= 1)
+  float* out_coup;     // [B][ring][2*ld] couplings (dense_level >= 2)
+  int ring;
+  double* log_t;       // [B][log_cap] accepted step times
+  double* log_h;       // [B][log_cap] step size after each accepted step
+  int log_cap;
+  long long max_attempts;       // per launch, < 0: unlimited
+  unsigned long long timeout_ns;
+  unsigned bar_extra;  // arrivals a barrier waits for beyond the grid (tests of the time limit)
+  float* fin_theta;    // [B][ld] end-of-run phases / RHS output
+  float* fin_coup;     // [B][2*ld]
+  long long* counters; // [0] barriers executed (CTA 0 adds)
+};
+
+enum Mode { MODE_INTEGRATE = 0, MODE_FINAL = 1, MODE_RHS = 2 };
+
+// The persistent kernel instantiations; bmax/kmax select the template.
+cudaError_t persistent_config(int coupling, int bmax, int kmax, size_t* smem_bytes, int* blocks_per_sm,
+                              int rows_per_cta);
+cudaError_t launch_persistent(const KParams& p, int grid, int bmax, int kmax, size_t smem, cudaStream_t st);
+cudaError_t launch_init_state(const float* theta, int n, int ld, float* hi, float* lo, long long* w,
+                              cudaStream_t st);
+cudaError_t launch_volcano_words(int seed, int n, int k, int words, uint32_t* bits, cudaStream_t st);
+cudaError_t launch_volcano_adjacency(const uint32_t* bits, int n, int k, int words, int ld, float* adj,
+                                     cudaStream_t st);
+cudaError_t launch_unwrap(const float* hi, const float* lo, const long long* w, int n, float* out,
+                          cudaStream_t st);
+
+}  // namespace kura

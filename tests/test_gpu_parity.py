@@ -1,0 +1,232 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Bit-exact where the work is integer or a single rounding (Philox factor bits,
+the dense volcano adjacency); within the stated tolerances where it is floating
+point: the RHS to float32 rounding, and whole adaptive runs against the FP64
+oracle with phases within 1e-4 rad for t <= 10 and the order parameter r within
+1e-4 (its time average within 1e-3 over the full horizon).
+"""
+import numpy as np
+import pytest
+
+from helpers import cauchy_inputs, normal_inputs
+
+pytestmark = pytest.mark.gpu
+
+DENSE, VOLCANO = 0, 1
+
+
+def make(native, n, k, coupling, theta, omega, c=3.0, batch=1, seed=1, dense_level=1, atol=1e-6, rtol=0.0,
+         fixed=False, t1=10.0, dt=1.0, h0=None, adj=None, thetas=None, cs=None):
+    net = native.Network(n, k=k, coupling=coupling, batch=batch, seed=seed, atol=atol, rtol=rtol, fixed_step=fixed,
+                         dense_level=dense_level)
+    net.set_frequencies(omega)
+    if coupling == DENSE:
+        if adj is None:
+            net.generate_adjacency()
+        else:
+            net.set_adjacency(adj)
+    for b in range(batch):
+        net.set_coupling(b, c if cs is None else cs[b])
+        net.set_state(b, theta if thetas is None else thetas[b], 0.0, dt / 100 if h0 is None else h0)
+    net.set_horizon(t1, dt, True)
+    return net
+
+
+def collect(net, batch=1):
+    rec = {b: {"theta": [], "coup": [], "r": [], "t": []} for b in range(batch)}
+    steps = {b: [] for b in range(batch)}
+
+    def on_out(b, idx, te, r, th, cp):
+        rec[b]["theta"].append(th)
+        rec[b]["coup"].append(cp)
+        rec[b]["r"].append(r)
+        rec[b]["t"].append(te)
+
+    def on_step(b, t, h, s):
+        steps[b].append((t, h))
+
+    net.run(on_step=on_step, on_output=on_out)
+    return rec, steps
+
+
+# ------------------------------------------------------------------ integer / single-rounding parity
+@pytest.mark.parametrize("seed,n,k", [(1, 1, 1), (1, 37, 5), (7, 1000, 8), (-3, 513, 33), (123456, 4099, 5)])
+def test_volcano_bits_bit_exact(native, oracle_lib, seed, n, k):
+    assert np.array_equal(native.volcano_factor(seed, n, k), oracle_lib.volcano_factor(seed, n, k))
+
+
+@pytest.mark.parametrize("n,k", [(1, 1), (5, 0), (100, 5), (257, 40), (1000, 6)])
+def test_dense_adjacency_bit_exact(native, oracle_lib, n, k):
+    net = native.Network(n, k=k, coupling=DENSE, seed=4)
+    net.generate_adjacency()
+    a = net.adjacency()
+    ref = oracle_lib.volcano_adjacency(4, n, k, fp64=False)
+    assert np.array_equal(a.view(np.uint32), ref.view(np.uint32))
+    net.close()
+
+
+# ------------------------------------------------------------------ RHS
+@pytest.mark.parametrize("coupling", [DENSE, VOLCANO])
+@pytest.mark.parametrize("n", [1, 33, 700])
+def test_rhs_matches_oracle(native, oracle_lib, coupling, n):
+    th, om = cauchy_inputs(n, 5)
+    th = th + np.float32(40.0) * (np.arange(n) % 3)  # unwrapped phases far from [0, 2pi)
+    net = native.Network(n, k=5, coupling=coupling, seed=3)
+    net.set_frequencies(om)
+    if coupling == DENSE:
+        net.generate_adjacency()
+    net.set_coupling(0, 2.5)
+    f, cp = net.rhs(0, th)
+    fr, cpr = oracle_lib.rhs(th, om, k=5, c1=2.5, onthefly=coupling == VOLCANO, seed=3, fp64=True)
+    assert np.max(np.abs(cp - cpr)) < 2e-6
+    assert np.all(np.abs(f - fr) <= 2e-5 + 1e-7 * np.abs(fr))
+    net.close()
+
+
+# ------------------------------------------------------------------ whole runs
+@pytest.mark.parametrize("coupling", [DENSE, VOLCANO])
+@pytest.mark.parametrize("n", [64, 500])
+def test_run_matches_fp64_oracle(native, oracle_lib, coupling, n):
+    th, om = cauchy_inputs(n, 21 + n)
+    net = make(native, n, 5, coupling, th, om, c=3.0, seed=2, dense_level=2, t1=10.0, dt=1.0)
+    rec, steps = collect(net)
+    ref = oracle_lib.run(th, om, k=5, c1=3.0, onthefly=coupling == VOLCANO, seed=2, fp64=True, t1=10.0, dt=1.0,
+                         dense=2)
+    r = np.array(rec[0]["r"])
+    assert r.size == ref.order.size == 11
+    assert np.max(np.abs(r - ref.order)) < 1e-4
+    theta = np.array(rec[0]["theta"])
+    dth = np.abs(theta.astype(np.float64) - ref.thetas)
+    assert np.max(dth) < 1e-4, np.max(dth)
+    coup = np.array(rec[0]["coup"])
+    assert np.max(np.abs(coup - ref.couplings)) < 1e-4
+    assert abs(len(steps[0]) - ref.steps) <= max(2, ref.steps // 50)
+    st = net.stats()
+    assert st["accepted"] == len(steps[0]) and st["launches"] >= 1
+    # end-of-run record (theta at the last t_eval with k1 replaced by k7), t and h
+    fth, fcp, ft, fh = net.final_record(0)
+    assert np.max(np.abs(fth.astype(np.float64) - ref.final_theta)) < 1e-4
+    assert np.max(np.abs(fcp - ref.final_coupling)) < 1e-4
+    assert ft == pytest.approx(ref.final_t, rel=1e-3)
+    net.close()
+
+
+@pytest.mark.parametrize("coupling", [DENSE, VOLCANO])
+def test_long_horizon_order_mean(native, oracle_lib, coupling):
+    n = 400
+    th, om = normal_inputs(n, 3)
+    net = make(native, n, 5, coupling, th, om, c=3.0, seed=6, dense_level=0, t1=100.0, dt=1.0)
+    net.run()
+    r = net.order(0)
+    ref = oracle_lib.run(th, om, k=5, c1=3.0, onthefly=coupling == VOLCANO, seed=6, fp64=True, t1=100.0, dt=1.0)
+    assert r.size == ref.order.size == 101
+    assert abs(r.mean() - ref.order.mean()) < 1e-3
+    assert np.max(np.abs(r[:11] - ref.order[:11])) < 1e-4
+    net.close()
+
+
+def test_batch_equals_separate_runs(native):
+    n = 300
+    th, om = normal_inputs(n, 8)
+    cs = [1.0, 2.0, 3.0, 4.0, 5.0]
+    net = make(native, n, 5, VOLCANO, th, om, batch=5, cs=cs, dense_level=0, t1=20.0, dt=1.0)
+    net.run()
+    rb = [net.order(b) for b in range(5)]
+    sb = [net.state(b) for b in range(5)]
+    net.close()
+    for b, c in enumerate(cs):
+        one = make(native, n, 5, VOLCANO, th, om, c=c, dense_level=0, t1=20.0, dt=1.0)
+        one.run()
+        assert np.array_equal(one.order(0), rb[b])
+        st = one.state(0)
+        assert np.array_equal(st[0], sb[b][0]) and st[1] == sb[b][1]
+        one.close()
+
+
+def test_dense_batch_matches_fp64(native, oracle_lib):
+    n = 200
+    thetas = [cauchy_inputs(n, 30 + b)[0] for b in range(3)]
+    _, om = cauchy_inputs(n, 29)
+    net = make(native, n, 5, DENSE, None, om, batch=3, thetas=thetas, dense_level=0, t1=10.0, dt=0.5)
+    net.run()
+    for b in range(3):
+        ref = oracle_lib.run(thetas[b], om, k=5, c1=3.0, fp64=True, t1=10.0, dt=0.5)
+        assert np.max(np.abs(net.order(b) - ref.order)) < 1e-4
+    net.close()
+
+
+@pytest.mark.parametrize("coupling", [DENSE, VOLCANO])
+def test_uncoupled_known_answer(native, coupling):
+    n = 1000
+    th, om = native.random_inputs(1, n, 0.0, 1.0, True)
+    net = make(native, n, 0, coupling, th, om, c=1.75, dense_level=1, t1=5.0, dt=0.01)
+    rec, _ = collect(net)
+    t = np.float32(0.01) * np.arange(1, 501, dtype=np.float32)
+    ph = np.outer(t.astype(np.float64), om.astype(np.float64))
+    theta = np.array(rec[0]["theta"][1:], np.float64)
+    assert theta.shape == ph.shape
+    assert np.max(np.abs(theta - ph) / (1 + np.abs(ph) * 1e-7)) < 1e-4
+    analytic = np.abs(np.exp(1j * ph).mean(1))
+    assert np.max(np.abs(np.array(rec[0]["r"][1:]) - analytic)) < 2e-6
+    net.close()
+
+
+def test_fixed_step_matches_oracle(native, oracle_lib):
+    n = 128
+    th, om = normal_inputs(n, 4)
+    net = make(native, n, 5, DENSE, th, om, fixed=True, h0=0.01, dense_level=1, t1=2.0, dt=0.5)
+    rec, steps = collect(net)
+    ref = oracle_lib.run(th, om, k=5, c1=3.0, fp64=True, fixed=True, h0=0.01, t1=2.0, dt=0.5, dense=1)
+    assert len(steps[0]) == ref.steps
+    assert np.max(np.abs(np.array(rec[0]["theta"]) - ref.thetas)) < 1e-4
+    net.close()
+
+
+def test_rtol_matches_oracle(native, oracle_lib):
+    n = 128
+    th, om = normal_inputs(n, 12)
+    net = make(native, n, 5, VOLCANO, th, om, rtol=1e-5, atol=1e-7, dense_level=0, t1=5.0, dt=1.0)
+    net.run()
+    ref = oracle_lib.run(th, om, k=5, c1=3.0, onthefly=True, fp64=True, rtol=1e-5, atol=1e-7, t1=5.0, dt=1.0)
+    assert np.max(np.abs(net.order(0) - ref.order)) < 1e-4
+    net.close()
+
+
+def test_explicit_adjacency(native, oracle_lib):
+    n = 90
+    rng = np.random.default_rng(3)
+    adj = (rng.standard_normal((n, n)) / n).astype(np.float32)
+    th, om = normal_inputs(n, 13)
+    net = make(native, n, 5, DENSE, th, om, adj=adj, dense_level=0, t1=5.0, dt=1.0)
+    net.run()
+    ref = oracle_lib.run(th, om, k=5, c1=3.0, adj=adj.astype(np.float64), fp64=True, t1=5.0, dt=1.0)
+    assert np.max(np.abs(net.order(0) - ref.order)) < 1e-4
+    net.close()
+
+
+def test_step_underflow_reports_error(native):
+    n = 64
+    th, om = normal_inputs(n, 2)
+    net = make(native, n, 5, VOLCANO, th, om, atol=1e-30, dense_level=0, t1=1.0, dt=1.0)
+    with pytest.raises(native.KuraError) as e:
+        net.run()
+    assert e.value.code == -5
+    net.close()
+
+
+def test_barrier_timeout_reports_error_and_context_survives(native, monkeypatch):
+    n = 256
+    th, om = normal_inputs(n, 2)
+    monkeypatch.setenv("KURA_BARRIER_TIMEOUT_MS", "300")
+    monkeypatch.setenv("KURA_TEST_BARRIER_EXTRA", "1")  # each barrier waits for one arrival that never comes
+    net = make(native, n, 5, VOLCANO, th, om, dense_level=0, t1=1.0, dt=1.0)
+    with pytest.raises(native.KuraError) as e:
+        net.run()
+    assert e.value.code == -4
+    net.close()
+    monkeypatch.delenv("KURA_TEST_BARRIER_EXTRA")
+    net = make(native, n, 5, VOLCANO, th, om, dense_level=0, t1=1.0, dt=1.0)
+    net.run()
+    assert net.order(0).size == 2
+    net.close()
