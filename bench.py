@@ -116,6 +116,25 @@ def dist_env():
     return ws, rank, local
 
 
+def instance_seed(rank):
+    """Each rank integrates its own network instance (weak scaling, no data exchange)."""
+    return 1 + rank
+
+
+def combine_ranks(units, ms, device):
+    """Whole-job units (sum over ranks) and time (max over ranks)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(units), float(ms)
+    t = torch.tensor([float(units), float(ms)], dtype=torch.float64, device=device)
+    u = t[:1].clone()
+    m = t[1:].clone()
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    return float(u.item()), float(m.item())
+
+
 def run_native(args, w):
     import torch
     import kuramoto_gb300 as kg
@@ -125,7 +144,7 @@ def run_native(args, w):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    seed = 1 + rank
+    seed = instance_seed(rank)
     thetas, om = inputs(w, seed)
     n, B = w["n"], len(w["cs"])
     stream = torch.cuda.current_stream()
@@ -175,11 +194,7 @@ def run_native(args, w):
     acc_per_step = st1["accepted"]
     launches = st1["launches"] - st0["launches"]
     kernel_ms = st1["kernel_ms"] - st0["kernel_ms"]
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    units = acc_per_step * n * args.steps * ws
+    units, ms = combine_ranks(acc_per_step * n * args.steps, ms, "cuda")
     value = units / (ms / 1e3)
     orders = [net.order(b) for b in range(B)]
 
@@ -206,7 +221,8 @@ def run_native(args, w):
         if it == 0:
             h2d = 4 * n + 4 * n * B
             d2h = sum(4 * r.size for r in rs) + 4 * n * B
-    e2e_value = acc_per_step * n * args.steps * ws / (e2e_ms / 1e3)
+    e2e_units, e2e_ms = combine_ranks(acc_per_step * n * args.steps, e2e_ms, "cuda")
+    e2e_value = e2e_units / (e2e_ms / 1e3)
     net.close()
     res = dict(value=value, ms=ms, wall=t_wall, kernel_ms=kernel_ms, launches=launches, acc_per_step=acc_per_step,
                e2e_value=e2e_value, h2d=h2d, d2h=d2h, clocks=clk.summary(), orders=orders, thetas=thetas, om=om,
@@ -276,8 +292,11 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--workload", default="volcano200k", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--t1", type=float, default=None, help="shorter horizon (profiling captures only)")
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.t1 is not None:
+        w["t1"] = args.t1
     ws, rank, local = dist_env()
     n, B = w["n"], len(w["cs"])
     config = {"workload": args.workload, "n": n, "k": w["k"], "coupling": "volcano-regenerated" if w["coupling"] else

@@ -61,7 +61,7 @@ struct kura_handle {
   long long* counters = nullptr;
   int ring = 0, ring_alloc = 0, ring_dl = -1, log_cap = 0, n_eval = 0, t_eval_alloc = 0;
   double dt = 1, t1 = 0;
-  int grid = 1, rows = 1;
+  int grid = 1, rows = 1, xs_smem = 0;
   size_t smem = 0;
   // host
   std::vector<TrajG> htraj;
@@ -181,13 +181,13 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   int G = sms;
   int rows = ceil_div(h->n, G);
   int bps = 0;
-  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows));
+  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));
   if (bps < 1) return bail(fail(KURA_ERR_UNSUPPORTED, "persistent kernel does not fit on an SM"));
   G = sms * std::min(bps, 1);
   G = std::min(G, std::max(1, ceil_div(h->n, 64)));
   rows = ceil_div(h->n, G);
   G = ceil_div(h->n, rows);
-  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows));
+  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));
   if (bps < 1) return bail(fail(KURA_ERR_UNSUPPORTED, "persistent kernel shared memory exceeds an SM"));
   h->grid = G;
   h->rows = rows;
@@ -407,6 +407,7 @@ static int launch(kura_handle* h, int mode, bool log_steps) {
   const char* extra = getenv("KURA_TEST_BARRIER_EXTRA");
   p.bar_extra = extra ? (unsigned)atoi(extra) : 0u;
   p.fin_theta = h->fin_theta; p.fin_coup = h->fin_coup;
+  p.xs_smem = h->xs_smem;
   p.counters = h->counters;
   CU(cudaMemcpyAsync(h->traj, h->htraj.data(), sizeof(TrajG) * h->B, cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(h->bar, 0, sizeof(unsigned), h->stream));

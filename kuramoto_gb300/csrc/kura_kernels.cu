@@ -163,7 +163,8 @@ __host__ __device__ constexpr int pw_of(int coup, int kmax) { return coup == KUR
 __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
 
 // shared-memory layout (bytes), also used by the host to size the launch
-__host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int rows, int* off, int* total) {
+__host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int rows, int xs_smem, int* off,
+                                            int* total) {
   int pw = pw_of(coup, kmax);
   int o = 0;
   off[0] = o; o += align16(bmax * (int)sizeof(TrajG));
@@ -176,6 +177,7 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
   off[7] = o; o += align16(coup == KURA_COUPLING_DENSE ? bmax * CT * 8 : 0); // x tile
   off[8] = o; o += align16(bmax * 2 * kmax * 4);         // f3 (volcano)
+  off[9] = o; o += align16(coup == KURA_COUPLING_VOLCANO && xs_smem ? bmax * rows * 8 : 0);  // own (cos, sin)
   *total = o;
 }
 
@@ -194,13 +196,14 @@ struct Engine {
   uint32_t* ubits;
   float2* xt;
   float* f3;
+  float2* xs;   // (cos, sin) of the CTA's rows, [b][rows]: shared memory, or the CTA's part of xbuf
   int G, gi, tid, lane, warp, r0, r1, B;
   unsigned target;
   int nbar, xpar;
 
   __device__ Engine(const KParams& pp, unsigned char* smem) : p(pp) {
-    int off[9], total;
-    smem_layout(COUP, BMAX, KMAX, pp.rows, off, &total);
+    int off[10], total;
+    smem_layout(COUP, BMAX, KMAX, pp.rows, pp.xs_smem, off, &total);
     tr = (TrajG*)(smem + off[0]);
     sb = (SrcB*)(smem + off[1]);
     red = (float*)(smem + off[2]);
@@ -221,6 +224,12 @@ struct Engine {
     target = 0;
     nbar = 0;
     xpar = 0;
+    xs = pp.xs_smem ? (float2*)(smem + off[9]) : nullptr;
+  }
+
+  // (cos, sin) of row i of trajectory b for the volcano coupling (own rows only)
+  __device__ __forceinline__ float2* xrow(int b) {
+    return xs ? xs + (size_t)b * p.rows - r0 : p.xbuf + (size_t)b * p.ld;
   }
 
   // Grid barrier with a time limit.  Returns false (on every thread) when the
@@ -258,30 +267,41 @@ struct Engine {
     return v;
   }
 
-  // red[warp][b][*] -> part[par][gi][b][*]
+  // red[warp][b][0..npw) summed over warps -> part[par][gi][b][0..npw)
   __device__ void publish_partials(int npw) {
     __syncthreads();
     int par = nbar & 1;
     for (int v = tid; v < B * npw; v += KT) {
-      int b = v / npw, w = v % npw;
+      int b = v / npw, w = v - b * npw;
       float s = 0.f;
+#pragma unroll
       for (int q = 0; q < KW; ++q) s += red[(q * BMAX + b) * PW + w];
       p.part[((size_t)(par * G + gi) * B + b) * PW_MAX + w] = s;
     }
   }
-  // part[par][*][b][w] summed over CTAs in a fixed order -> rsum[b*PW + w]
+  // part[par][*][b][w] summed over CTAs in a fixed order -> rsum[b*PW + w].  The
+  // CTAs are split into slices that threads sum in parallel; each thread issues its
+  // loads 16 at a time so their latencies overlap.
   __device__ void gather_partials(int npw) {
-    int par = (nbar - 1) & 1;  // the parity published before the barrier just passed
-    int NV = B * npw;
+    const int par = (nbar - 1) & 1;  // the parity published before the barrier just passed
+    const int NV = B * npw;
     int S = KT / NV;
     if (S < 1) S = 1;
     if (S > G) S = G;
+    const size_t stride = (size_t)B * PW_MAX;
     for (int t = tid; t < S * NV; t += KT) {
       int v = t % NV, sl = t / NV;
-      int b = v / npw, w = v % npw;
+      int b = v / npw, w = v - b * npw;
       int g0 = (int)((long long)sl * G / S), g1 = (int)((long long)(sl + 1) * G / S);
+      const float* src = p.part + ((size_t)par * G * B + b) * PW_MAX + w;
       float s = 0.f;
-      for (int g = g0; g < g1; ++g) s += __ldcg(&p.part[((size_t)(par * G + g) * B + b) * PW_MAX + w]);
+      for (int g = g0; g < g1; g += 16) {
+        float v16[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) v16[u] = (g + u < g1) ? __ldcg(src + (size_t)(g + u) * stride) : 0.f;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) s += v16[u];
+      }
       slice[sl * NV + v] = s;
     }
     __syncthreads();
@@ -316,8 +336,9 @@ struct Engine {
 
   // ---- one coupling evaluation for every active trajectory (one grid barrier)
   __device__ bool coupling_eval(bool want_r) {
-    const int n = p.n, ld = p.ld;
+    const int n = p.n, ld = p.ld, k = p.k;
     const bool need_part = (COUP == KURA_COUPLING_VOLCANO) || want_r;
+    const int npw = (COUP == KURA_COUPLING_VOLCANO ? 2 * k : 0) + (want_r ? 2 : 0);
     // phase A: stage value, sincos, exchange data and partial sums
     for (int b = 0; b < B; ++b) {
       const SrcB& s = sb[b];
@@ -327,6 +348,10 @@ struct Engine {
       if (s.active) {
         const float* hiB = p.ph_hi + ((size_t)s.base * B + b) * ld;
         const float* loB = p.ph_lo + ((size_t)s.base * B + b) * ld;
+        float2* xo = (COUP == KURA_COUPLING_VOLCANO) ? xrow(b) : p.xbuf + ((size_t)xpar * B + b) * ld;
+        const bool keep_y7 = s.store_y7;
+        const bool emit = s.rec && ((p.dense_level >= 1 && p.mode == MODE_INTEGRATE) || p.mode == MODE_FINAL);
+#pragma unroll 2
         for (int i = r0 + tid; i < r1; i += KT) {
           float om = p.omega[i];
           float gsum = 0.f;
@@ -339,11 +364,11 @@ struct Engine {
           float arg = reduce_arg(s2.hi, lo);
           float sn, cs;
           sincosf(arg, &sn, &cs);
-          p.xbuf[((size_t)xpar * B + b) * ld + i] = make_float2(cs, sn);
-          if (s.store_y7 || (s.rec && p.dense_level >= 1 && p.mode == MODE_INTEGRATE) || (s.rec && p.mode == MODE_FINAL)) {
+          xo[i] = make_float2(cs, sn);
+          if (keep_y7 || emit) {
             f2 y = two_sum(s2.hi, lo);
             long long w = p.ph_w[((size_t)s.base * B + b) * ld + i];
-            if (s.store_y7) {
+            if (keep_y7) {
               float hi7 = y.hi, lo7 = y.lo;
               long long w7 = w;
               wrap_phase(hi7, lo7, w7);
@@ -363,7 +388,7 @@ struct Engine {
             uint32_t u = ubits[i - r0];
 #pragma unroll
             for (int m = 0; m < KMAX; ++m) {
-              if (m < p.k) {
+              if (m < k) {
                 float sg = ((u >> m) & 1u) ? 1.f : -1.f;
                 acc[2 * m] = __fmaf_rn(sg, cs, acc[2 * m]);
                 acc[2 * m + 1] = __fmaf_rn(sg, sn, acc[2 * m + 1]);
@@ -377,16 +402,30 @@ struct Engine {
         }
       }
       if (need_part) {
+        // compact layout: [2k projections][sum cos, sum sin]
+        float* dst = red + (warp * BMAX + b) * PW;
+        if (COUP == KURA_COUPLING_VOLCANO) {
 #pragma unroll
-        for (int v = 0; v < PW; ++v) {
-          float t = warp_sum(acc[v]);
-          if (lane == 0) red[(warp * BMAX + b) * PW + v] = t;
+          for (int v = 0; v < 2 * KMAX; ++v) {
+            if (v < 2 * k) {
+              float t = warp_sum(acc[v]);
+              if (lane == 0) dst[v] = t;
+            }
+          }
+        }
+        if (want_r) {
+          float t0 = warp_sum(acc[PW - 2]);
+          float t1 = warp_sum(acc[PW - 1]);
+          if (lane == 0) {
+            dst[npw - 2] = t0;
+            dst[npw - 1] = t1;
+          }
         }
       }
     }
-    if (need_part) publish_partials(PW);
+    if (need_part) publish_partials(npw);
     if (!grid_sync()) return false;
-    if (need_part) gather_partials(PW);
+    if (need_part) gather_partials(npw);
 
     // phase C: couplings for the CTA's rows
     if (COUP == KURA_COUPLING_VOLCANO) {
@@ -395,20 +434,21 @@ struct Engine {
         int b = v / (2 * KMAX), w = v % (2 * KMAX);
         int m = w >> 1;
         float sgn = (m & 1) ? -1.f : 1.f;
-        f3[v] = (m < p.k) ? (sgn * rsum[b * PW + w]) / (float)n : 0.f;
+        f3[v] = (m < k) ? (sgn * rsum[b * PW + w]) / (float)n : 0.f;
       }
       __syncthreads();
       for (int b = 0; b < B; ++b) {
         if (!sb[b].active) continue;
-        const float2* xb = p.xbuf + ((size_t)xpar * B + b) * ld;
+        const float2* xb = xrow(b);
         const float* fb = f3 + b * 2 * KMAX;
+#pragma unroll 2
         for (int i = r0 + tid; i < r1; i += KT) {
           uint32_t u = ubits[i - r0];
           float Fc = 0.f, Fs = 0.f;
           // m2 (kuramoto.cu:83-101): F_n = sum_m u_mn f3_m, sequential in m
 #pragma unroll
           for (int m = 0; m < KMAX; ++m) {
-            if (m < p.k) {
+            if (m < k) {
               bool pos = (u >> m) & 1u;
               Fc += pos ? fb[2 * m] : -fb[2 * m];
               Fs += pos ? fb[2 * m + 1] : -fb[2 * m + 1];
@@ -421,11 +461,11 @@ struct Engine {
     } else {
       dense_matvec();
     }
-    if (want_r && gi == 0 && tid == 0) {
-      for (int b = 0; b < B; ++b) {
-        const SrcB& s = sb[b];
-        if (!s.active || !s.rec || p.mode != MODE_INTEGRATE) continue;
-        float X = rsum[b * PW + PW - 2], Y = rsum[b * PW + PW - 1];
+    if (want_r && gi == 0 && tid < B) {
+      const int b = tid;
+      const SrcB& s = sb[b];
+      if (s.active && s.rec && p.mode == MODE_INTEGRATE) {
+        float X = rsum[b * PW + npw - 2], Y = rsum[b * PW + npw - 1];
         float xn = X / (float)n, yn = Y / (float)n;
         p.out_r[(size_t)b * p.ring + s.oslot] = sqrtf(xn * xn + yn * yn);
         p.out_idx[(size_t)b * p.ring + s.oslot] = s.oidx;
@@ -522,11 +562,7 @@ struct Engine {
         }
       }
       float t = warp_sum(acc);
-      if (lane == 0) {
-        red[(warp * BMAX + b) * PW] = t;
-#pragma unroll
-        for (int v = 1; v < PW; ++v) red[(warp * BMAX + b) * PW + v] = 0.f;
-      }
+      if (lane == 0) red[(warp * BMAX + b) * PW] = t;
     }
     publish_partials(1);
     if (!grid_sync()) return false;
@@ -534,64 +570,118 @@ struct Engine {
     return true;
   }
 
-  // ---- per-trajectory sources (thread 0 only)
-  __device__ void set_stage_src(int b, int s, float hf) {
-    SrcB& S = sb[b];
-    const TrajG& T = tr[b];
-    for (int j = 0; j < 7; ++j) S.W[j] = 0.f;
-    for (int j = 0; j < s - 1; ++j) S.W[j] = (float)((double)hf * A_TAB[s - 1][j]);
-    S.nW = s - 1;
-    double mh = C_TAB[s - 1] * (double)hf;
-    S.m_hi = (float)mh;
-    S.m_lo = (float)(mh - (double)S.m_hi);
-    S.slot[0] = slot_k1(T.rot_g);
-    for (int j = 1; j < 6; ++j) S.slot[j] = j;
-    S.slot[6] = slot_k7(T.rot_g);
-    S.base = T.rot_y;
-    S.gout = (s < 7) ? s - 1 : slot_k7(T.rot_g);
-    S.store_y7 = (s == 7);
-    S.rec = 0;
-    S.oslot = -1;
-    S.oidx = 0;
-    for (int j = 0; j < 7; ++j) S.E[j] = (float)((double)hf * E_TAB[j]);
-  }
-  // dense output at t_eval from the last accepted step (interpolate, dp45.cu:70-76).
-  // k1_slot / k7_slot choose the physical slopes; the end-of-run record passes the
-  // slot of k7 for both, as the reference's FSAL copy leaves it (dp45.cu:160).
-  __device__ void set_eval_src(int b, double te, int k1_slot, int k7_slot) {
-    SrcB& S = sb[b];
-    const TrajG& T = tr[b];
-    double hs = T.t - T.t_last;
-    double dl = te - T.t_last;
-    double x = dl / hs;
-    for (int j = 0; j < 7; ++j) {
-      double c = P_TAB[j][0] * x + P_TAB[j][1] * x * x + P_TAB[j][2] * x * x * x + P_TAB[j][3] * x * x * x * x;
-      S.W[j] = (float)(hs * c);
+  // ---- per-trajectory sources, filled by 16 threads per trajectory
+  // stage s of the attempt (the stage loop of dp45_step, dp45.cu:90-106)
+  __device__ void setup_stage(int s) {
+    if (tid < B * 16) {
+      const int b = tid >> 4, j = tid & 15;
+      SrcB& S = sb[b];
+      const TrajG& T = tr[b];
+      const double h = T.h;
+      if (j < 7) {
+        S.W[j] = (j < s - 1) ? (float)(h * A_TAB[s - 1][j]) : 0.f;
+      } else if (j < 14) {
+        if (s == 7) S.E[j - 7] = (float)(h * E_TAB[j - 7]);
+      } else if (j == 14) {
+        double mh = C_TAB[s - 1] * h;
+        float hi = (float)mh;
+        S.m_hi = hi;
+        S.m_lo = (float)(mh - (double)hi);
+      } else {
+        S.nW = s - 1;
+        S.slot[0] = slot_k1(T.rot_g);
+        for (int q = 1; q < 6; ++q) S.slot[q] = q;
+        S.slot[6] = slot_k7(T.rot_g);
+        S.base = T.rot_y;
+        S.gout = (s < 7) ? s - 1 : slot_k7(T.rot_g);
+        S.store_y7 = (s == 7);
+        S.rec = 0;
+        S.oslot = -1;
+        S.oidx = 0;
+      }
     }
-    S.nW = 7;
-    S.m_hi = (float)dl;
-    S.m_lo = (float)(dl - (double)S.m_hi);
-    S.slot[0] = k1_slot;
-    for (int j = 1; j < 6; ++j) S.slot[j] = j;
-    S.slot[6] = k7_slot;
-    S.base = T.rot_y ^ 1;
-    S.gout = -1;
-    S.store_y7 = 0;
-    S.rec = 1;
+    __syncthreads();
   }
-  __device__ void set_y_src(int b) {
+  // dense output at te from the last accepted step (interpolate, dp45.cu:70-76).
+  // k1s / k7s choose the physical slopes; the end-of-run record passes the slot of
+  // k7 for both, as the reference's FSAL copy leaves them (dp45.cu:160).
+  __device__ void fill_eval(int b, int j, double te, int k1s, int k7s) {
     SrcB& S = sb[b];
     const TrajG& T = tr[b];
-    for (int j = 0; j < 7; ++j) S.W[j] = 0.f;
-    S.nW = 0;
-    S.m_hi = S.m_lo = 0.f;
-    for (int j = 0; j < 7; ++j) S.slot[j] = j;
-    S.base = T.rot_y;
-    S.gout = -1;
-    S.store_y7 = 0;
-    S.rec = 0;
-    S.oslot = -1;
-    S.oidx = -1;
+    const double hs = T.t - T.t_last, dl = te - T.t_last;
+    if (j < 7) {
+      const double x = dl / hs;
+      const double c = ((P_TAB[j][3] * x + P_TAB[j][2]) * x + P_TAB[j][1]) * x * x + P_TAB[j][0] * x;
+      S.W[j] = (float)(hs * c);
+    } else if (j == 14) {
+      float hi = (float)dl;
+      S.m_hi = hi;
+      S.m_lo = (float)(dl - (double)hi);
+    } else if (j == 15) {
+      S.nW = 7;
+      S.slot[0] = k1s;
+      for (int q = 1; q < 6; ++q) S.slot[q] = q;
+      S.slot[6] = k7s;
+      S.base = T.rot_y ^ 1;
+      S.gout = -1;
+      S.store_y7 = 0;
+      S.rec = 1;
+    }
+  }
+  __device__ void fill_y(int b, int j) {
+    SrcB& S = sb[b];
+    const TrajG& T = tr[b];
+    if (j < 7) {
+      S.W[j] = 0.f;
+    } else if (j == 14) {
+      S.m_hi = S.m_lo = 0.f;
+    } else if (j == 15) {
+      S.nW = 0;
+      for (int q = 0; q < 7; ++q) S.slot[q] = q;
+      S.base = T.rot_y;
+      S.gout = -1;
+      S.store_y7 = 0;
+      S.rec = 0;
+      S.oslot = -1;
+      S.oidx = -1;
+    }
+  }
+
+  // controller of one trajectory after the error norm (dp45.cu:109-139)
+  __device__ void decide(int b) {
+    TrajG& T = tr[b];
+    const double h = T.h;
+    bool accept = true;
+    double factor = 1.0;
+    if (!p.fixed) {
+      double norm = sqrt((double)rsum[b * PW]) / sqrt((double)p.n);
+      if (isnan(norm)) {
+        T.status = KURA_ERR_NONFINITE;
+        return;
+      }
+      factor = 0.9 * pow(norm, -0.2);  // norm = +inf gives 0: the attempt is rejected with the 0.2 floor
+      accept = norm < 1.0;
+    }
+    if (accept) {
+      T.t_last = T.t;
+      T.t = T.t + h;
+      T.rot_y ^= 1;
+      T.rot_g ^= 1;
+      T.accepted++;
+      if (!p.fixed) T.h = h * fmin(factor, 10.0);
+      int e = T.eval_i;
+      while (e < p.n_eval && T.t >= (double)p.t_eval[e]) e++;
+      T.eval_end = e;
+      if (p.log_cap > 0) {
+        p.log_t[(size_t)b * p.log_cap + T.log_count] = T.t;
+        p.log_h[(size_t)b * p.log_cap + T.log_count] = T.h;
+      }
+      T.log_count++;
+    } else {
+      T.rejected++;
+      if (factor < 1.0) T.h = h * fmax(factor, 0.2);
+      if (!(T.h >= 1e-14 * fmax(1.0, fabs(T.t)))) T.status = KURA_ERR_STEP_UNDERFLOW;
+    }
   }
 
   __device__ void write_back() {
@@ -614,18 +704,19 @@ struct Engine {
     __syncthreads();
 
     if (p.mode == MODE_FINAL || p.mode == MODE_RHS) {
-      if (tid == 0) {
-        for (int b = 0; b < B; ++b) {
-          const TrajG& T = tr[b];
-          set_y_src(b);
-          SrcB& S = sb[b];
-          S.active = 1;
-          S.rec = 1;
-          if (p.mode == MODE_FINAL && p.n_eval > 0 && T.accepted > 0) {
-            int ks = slot_k1(T.rot_g);  // after the last FSAL swap this slot holds k7
-            set_eval_src(b, (double)p.t_eval[p.n_eval - 1], ks, ks);
-            S.active = 1;
-          }
+      if (tid < B * 16) {
+        const int b = tid >> 4, j = tid & 15;
+        const TrajG& T = tr[b];
+        if (p.mode == MODE_FINAL && p.n_eval > 0 && T.accepted > 0) {
+          int ks = slot_k1(T.rot_g);  // after the last FSAL swap this slot holds k7
+          fill_eval(b, j, (double)p.t_eval[p.n_eval - 1], ks, ks);
+        } else {
+          fill_y(b, j);
+        }
+        if (j == 15) {
+          sb[b].active = 1;
+          sb[b].rec = 1;
+          sb[b].oslot = -1;
         }
       }
       __syncthreads();
@@ -635,38 +726,38 @@ struct Engine {
     }
 
     // first slope of the run (dp45.cu:151) and the record at t0 (kuramoto.cu:587-626)
-    if (tid == 0) {
-      int any = 0;
-      for (int b = 0; b < B; ++b) {
-        TrajG& T = tr[b];
-        set_y_src(b);
+    if (tid < B * 16) {
+      const int b = tid >> 4, j = tid & 15;
+      const TrajG& T = tr[b];
+      fill_y(b, j);
+      if (j == 15) {
         SrcB& S = sb[b];
         S.active = (T.status == 0 && T.need_k1);
-        if (S.active) {
-          S.gout = slot_k1(T.rot_g);
-          if (T.need_init && T.out_count < p.ring) {
-            S.rec = 1;
-            S.oslot = T.out_count;
-            S.oidx = -1;
-          }
-          any = 1;
+        S.gout = slot_k1(T.rot_g);
+        if (S.active && T.need_init && T.out_count < p.ring) {
+          S.rec = 1;
+          S.oslot = T.out_count;
+          S.oidx = -1;
         }
       }
-      flag[1] = any;
     }
     __syncthreads();
-    if (flag[1]) {
-      bool want_r = false;
-      for (int b = 0; b < B; ++b) want_r |= (sb[b].active && sb[b].rec);
-      if (!coupling_eval(want_r)) return;
-      if (tid == 0) {
-        for (int b = 0; b < B; ++b) {
-          if (!sb[b].active) continue;
-          tr[b].need_k1 = 0;
-          if (sb[b].rec) { tr[b].need_init = 0; tr[b].out_count++; }
-        }
+    {
+      bool any = false, want_r = false;
+      for (int b = 0; b < B; ++b) {
+        any |= (bool)sb[b].active;
+        want_r |= (sb[b].active && sb[b].rec);
       }
-      __syncthreads();
+      if (any) {
+        if (!coupling_eval(want_r)) return;
+        if (tid < B) {
+          if (sb[tid].active) {
+            tr[tid].need_k1 = 0;
+            if (sb[tid].rec) { tr[tid].need_init = 0; tr[tid].out_count++; }
+          }
+        }
+        __syncthreads();
+      }
     }
 
     long long attempts = 0;
@@ -688,26 +779,29 @@ struct Engine {
         flag[1] = todo_out;
         flag[2] = todo_step;
         flag[3] = stop;
-        if (todo_out) {
-          for (int b = 0; b < B; ++b) {
-            TrajG& T = tr[b];
-            SrcB& S = sb[b];
-            S.active = (T.status == 0 && T.eval_i < T.eval_end && T.out_count < p.ring);
-            if (S.active) {
-              // after the accept, k1 of the step sits in the k7 slot and vice versa
-              set_eval_src(b, (double)p.t_eval[T.eval_i], slot_k7(T.rot_g), slot_k1(T.rot_g));
-              S.oslot = T.out_count;
-              S.oidx = T.eval_i;
-            }
-          }
-        }
       }
       __syncthreads();
       if (flag[1]) {
+        // one pending output of every trajectory that owes one
+        if (tid < B * 16) {
+          const int b = tid >> 4, j = tid & 15;
+          const TrajG& T = tr[b];
+          const bool act = (T.status == 0 && T.eval_i < T.eval_end && T.out_count < p.ring);
+          if (act) {
+            // after the accept, k1 of the step sits in the k7 slot and vice versa
+            fill_eval(b, j, (double)p.t_eval[T.eval_i], slot_k7(T.rot_g), slot_k1(T.rot_g));
+            if (j == 15) {
+              sb[b].oslot = T.out_count;
+              sb[b].oidx = T.eval_i;
+            }
+          }
+          if (j == 15) sb[b].active = act;
+        }
+        __syncthreads();
         if (!coupling_eval(true)) return;
-        if (tid == 0) {
-          for (int b = 0; b < B; ++b)
-            if (sb[b].active) { tr[b].eval_i++; tr[b].out_count++; }
+        if (tid < B && sb[tid].active) {
+          tr[tid].eval_i++;
+          tr[tid].out_count++;
         }
         __syncthreads();
         continue;
@@ -715,63 +809,19 @@ struct Engine {
       if (flag[3] || !flag[2]) break;
 
       // ---- one attempt of every stepping trajectory (dp45_step, dp45.cu:87-141)
-      if (tid == 0) {
-        for (int b = 0; b < B; ++b) {
-          const TrajG& T = tr[b];
-          sb[b].active = (T.status == 0 && T.eval_i >= T.eval_end && T.t < T.t1 &&
+      if (tid < B) {
+        const TrajG& T = tr[tid];
+        sb[tid].active = (T.status == 0 && T.eval_i >= T.eval_end && T.t < T.t1 &&
                           !(p.log_cap > 0 && T.log_count >= p.log_cap));
-        }
       }
-      __syncthreads();
       for (int s = 2; s <= 7; ++s) {
-        if (tid == 0) {
-          for (int b = 0; b < B; ++b) {
-            int act = sb[b].active;
-            set_stage_src(b, s, (float)tr[b].h);
-            sb[b].active = act;
-          }
-        }
-        __syncthreads();
+        setup_stage(s);  // ends with __syncthreads
         if (!coupling_eval(false)) return;
       }
       if (!p.fixed) {
         if (!error_phase()) return;
       }
-      if (tid == 0) {
-        for (int b = 0; b < B; ++b) {
-          if (!sb[b].active) continue;
-          TrajG& T = tr[b];
-          float hf = (float)T.h;
-          bool accept = true;
-          double factor = 1.0;
-          if (!p.fixed) {
-            double norm = sqrt((double)rsum[b * PW]) / sqrt((double)p.n);
-            if (!isfinite(norm)) { T.status = KURA_ERR_NONFINITE; continue; }
-            factor = 0.9 * pow(norm, -0.2);
-            accept = norm < 1.0;
-          }
-          if (accept) {
-            T.t_last = T.t;
-            T.t = T.t + (double)hf;
-            T.rot_y ^= 1;
-            T.rot_g ^= 1;
-            T.accepted++;
-            if (!p.fixed) T.h = (double)hf * fmin(factor, 10.0);
-            int e = T.eval_i;
-            while (e < p.n_eval && T.t >= (double)p.t_eval[e]) e++;
-            T.eval_end = e;
-            if (p.log_cap > 0) {
-              p.log_t[(size_t)b * p.log_cap + T.log_count] = T.t;
-              p.log_h[(size_t)b * p.log_cap + T.log_count] = T.h;
-            }
-            T.log_count++;
-          } else {
-            T.rejected++;
-            if (factor < 1.0) T.h = (double)hf * fmax(factor, 0.2);
-            if (!(T.h >= 1e-14 * fmax(1.0, fabs(T.t)))) T.status = KURA_ERR_STEP_UNDERFLOW;
-          }
-        }
-      }
+      if (tid < B && sb[tid].active) decide(tid);
       __syncthreads();
       attempts++;
     }
@@ -805,11 +855,18 @@ static const void* pick_kernel(int coupling, int bmax, int kmax) {
 }
 
 cudaError_t persistent_config(int coupling, int bmax, int kmax, size_t* smem_bytes, int* blocks_per_sm,
-                              int rows_per_cta) {
+                              int rows_per_cta, int* xs_smem) {
   const void* f = pick_kernel(coupling, bmax, kmax);
   if (!f) return cudaErrorInvalidValue;
-  int off[9], total;
-  smem_layout(coupling, bmax, coupling == KURA_COUPLING_DENSE ? 1 : kmax, rows_per_cta, off, &total);
+  int off[10], total;
+  const int kk = coupling == KURA_COUPLING_DENSE ? 1 : kmax;
+  // keep the CTA's (cos, sin) in shared memory when it fits comfortably
+  *xs_smem = 1;
+  smem_layout(coupling, bmax, kk, rows_per_cta, 1, off, &total);
+  if (coupling != KURA_COUPLING_VOLCANO || total > 200 * 1024) {
+    *xs_smem = 0;
+    smem_layout(coupling, bmax, kk, rows_per_cta, 0, off, &total);
+  }
   *smem_bytes = (size_t)total;
   cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, total);
   if (e != cudaSuccess) return e;

@@ -55,6 +55,7 @@ struct KParams {
   int log_cap;
   long long max_attempts;       // per launch, < 0: unlimited
   unsigned long long timeout_ns;
+  int xs_smem;         // 1: the CTA's (cos, sin) live in shared memory (volcano coupling)
   unsigned bar_extra;  // arrivals a barrier waits for beyond the grid (tests of the time limit)
   float* fin_theta;    // [B][ld] end-of-run phases / RHS output
   float* fin_coup;     // [B][2*ld]
@@ -65,7 +66,7 @@ enum Mode { MODE_INTEGRATE = 0, MODE_FINAL = 1, MODE_RHS = 2 };
 
 // The persistent kernel instantiations; bmax/kmax select the template.
 cudaError_t persistent_config(int coupling, int bmax, int kmax, size_t* smem_bytes, int* blocks_per_sm,
-                              int rows_per_cta);
+                              int rows_per_cta, int* xs_smem);
 cudaError_t launch_persistent(const KParams& p, int grid, int bmax, int kmax, size_t smem, cudaStream_t st);
 cudaError_t launch_init_state(const float* theta, int n, int ld, float* hi, float* lo, long long* w,
                               cudaStream_t st);

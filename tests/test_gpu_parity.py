@@ -16,6 +16,10 @@ pytestmark = pytest.mark.gpu
 DENSE, VOLCANO = 0, 1
 
 
+def f32_ulp(x):
+    return np.spacing(np.abs(np.asarray(x)).astype(np.float32)).astype(np.float64)
+
+
 def make(native, n, k, coupling, theta, omega, c=3.0, batch=1, seed=1, dense_level=1, atol=1e-6, rtol=0.0,
          fixed=False, t1=10.0, dt=1.0, h0=None, adj=None, thetas=None, cs=None):
     net = native.Network(n, k=k, coupling=coupling, batch=batch, seed=seed, atol=atol, rtol=rtol, fixed_step=fixed,
@@ -98,7 +102,16 @@ def test_run_matches_fp64_oracle(native, oracle_lib, coupling, n):
     assert np.max(np.abs(r - ref.order)) < 1e-4
     theta = np.array(rec[0]["theta"])
     dth = np.abs(theta.astype(np.float64) - ref.thetas)
-    assert np.max(dth) < 1e-4, np.max(dth)
+    # 1e-4 rad plus one float32 ulp of the unwrapped phase (the storage of thetas.dat).  A fast
+    # Cauchy outlier (|omega| h >> 1 rad per step) is under-resolved by the RMS error control of
+    # the method itself; its phase then depends on the exact step sequence.  For those, the bound
+    # is twice the FP64 oracle's own change under a 1e-9 relative change of the first step.
+    alt = oracle_lib.run(th, om, k=5, c1=3.0, onthefly=coupling == VOLCANO, seed=2, fp64=True, t1=10.0, dt=1.0,
+                         dense=2, h0=0.01 * (1 + 1e-9))
+    sens = np.abs(alt.thetas - ref.thetas)
+    tol = 1e-4 + f32_ulp(ref.thetas) + 2 * sens
+    assert np.all(dth <= tol), np.max(dth - tol)
+    assert np.mean(dth <= 1e-4 + f32_ulp(ref.thetas)) > 0.99
     coup = np.array(rec[0]["coup"])
     assert np.max(np.abs(coup - ref.couplings)) < 1e-4
     assert abs(len(steps[0]) - ref.steps) <= max(2, ref.steps // 50)
@@ -106,7 +119,8 @@ def test_run_matches_fp64_oracle(native, oracle_lib, coupling, n):
     assert st["accepted"] == len(steps[0]) and st["launches"] >= 1
     # end-of-run record (theta at the last t_eval with k1 replaced by k7), t and h
     fth, fcp, ft, fh = net.final_record(0)
-    assert np.max(np.abs(fth.astype(np.float64) - ref.final_theta)) < 1e-4
+    ftol = 1e-4 + f32_ulp(ref.final_theta) + 2 * np.abs(alt.final_theta - ref.final_theta)
+    assert np.all(np.abs(fth.astype(np.float64) - ref.final_theta) <= ftol)
     assert np.max(np.abs(fcp - ref.final_coupling)) < 1e-4
     assert ft == pytest.approx(ref.final_t, rel=1e-3)
     net.close()
@@ -179,7 +193,7 @@ def test_fixed_step_matches_oracle(native, oracle_lib):
     rec, steps = collect(net)
     ref = oracle_lib.run(th, om, k=5, c1=3.0, fp64=True, fixed=True, h0=0.01, t1=2.0, dt=0.5, dense=1)
     assert len(steps[0]) == ref.steps
-    assert np.max(np.abs(np.array(rec[0]["theta"]) - ref.thetas)) < 1e-4
+    assert np.all(np.abs(np.array(rec[0]["theta"]) - ref.thetas) <= 1e-4 + f32_ulp(ref.thetas))
     net.close()
 
 
