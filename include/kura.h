@@ -125,6 +125,26 @@ int kura_random_inputs(int32_t seed, int64_t n, float init, float freq, int32_t 
 /* Philox4x32-10 volcano factor bits as +/-1 int8 at m*n+i (kuramoto.cu:62-101, 128-135), on the device */
 int kura_volcano_factor(int32_t seed, int64_t n, int32_t k, int8_t* u);
 
+/* Integrates `batch` trajectories of one volcano network with the factor
+ * regenerated from Philox (the reference's -A mode) from t = 0 to t1, without
+ * allocating any device memory.  No counterpart in the reference.  For callers
+ * that cannot call cudaMalloc (a framework that owns the device allocator, a fixed
+ * device-memory budget, code that must not allocate while a graph is captured).
+ * Inputs and outputs are the caller's device buffers: omega_dev[n];
+ * theta_dev[batch][n] holds theta0 on entry and the final phases on return;
+ * order_dev[batch][order_cap] receives r(0) and r at t = dt, 2dt, .., int(t1/dt)*dt.
+ * c[batch] (coupling constants) is a host array; accepted (optional, host) gets the
+ * accepted steps summed over the batch.  Scratch is one static __device__ array of
+ * about 6.7 MiB held by every GPU that loads the library; it limits
+ * round_up(n,32)*batch <= 65536, batch <= 8, k <= 32 and order_cap <= 4096, and larger
+ * requests return KURA_ERR_INVALID.  All calls share that array: calls that overlap
+ * on the GPU race.  The first call on a device looks up the array's address; make it
+ * before any stream capture.  stream may be NULL (the legacy default stream). */
+int kura_integrate_volcano_noalloc(int64_t n, int32_t k, int32_t batch, int32_t seed, const float* c,
+                                   const float* omega_dev, float* theta_dev, double t1, double dt, double h0,
+                                   double atol, double rtol, int32_t device, void* stream, float* order_dev,
+                                   int64_t order_cap, int64_t* accepted);
+
 #ifdef __cplusplus
 }
 #endif

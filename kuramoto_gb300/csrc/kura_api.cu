@@ -75,6 +75,7 @@ struct kura_handle {
 };
 
 extern "C" const char* kura_last_error(void) { return g_err.c_str(); }
+void kura::set_last_error(const char* msg) { g_err = msg; }
 
 static int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 

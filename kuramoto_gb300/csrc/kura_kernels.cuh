@@ -73,6 +73,8 @@ cudaError_t launch_init_state(const float* theta, int n, int ld, float* hi, floa
 cudaError_t launch_volcano_words(int seed, int n, int k, int words, uint32_t* bits, cudaStream_t st);
 cudaError_t launch_volcano_adjacency(const uint32_t* bits, int n, int k, int words, int ld, float* adj,
                                      cudaStream_t st);
+// sets the message returned by kura_last_error() for the calling thread
+void set_last_error(const char* msg);
 cudaError_t launch_unwrap(const float* hi, const float* lo, const long long* w, int n, float* out,
                           cudaStream_t st);
 
