@@ -185,7 +185,9 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));
   if (bps < 1) return bail(fail(KURA_ERR_UNSUPPORTED, "persistent kernel does not fit on an SM"));
   G = sms * std::min(bps, 1);
-  G = std::min(G, std::max(1, ceil_div(h->n, 64)));
+  // at least 64 rows per CTA for the regenerated coupling (its cost per CTA is mostly
+  // fixed); 16 for the dense one, whose rows are long
+  G = std::min(G, std::max(1, ceil_div(h->n, h->coupling == KURA_COUPLING_DENSE ? 16 : 64)));
   rows = ceil_div(h->n, G);
   G = ceil_div(h->n, rows);
   CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));

@@ -96,6 +96,37 @@ __device__ __forceinline__ void wrap_phase(float& hi, float& lo, long long& w) {
   }
 }
 
+// sin and cos of hi + lo.  Cody-Waite reduction by pi/2 (three-part constant; the
+// first FMA is exact for |q| < 2^24) to r in about [-pi/4, pi/4], then the Taylor
+// series of sin (to r^9) and cos (to r^10) in Horner form: truncation error below
+// 2e-9 at |r| = pi/4, total error about 1e-7 absolute.
+constexpr double PIO2_D = 1.5707963267948966192313216916398;
+constexpr float PO2_1 = (float)PIO2_D;
+constexpr float PO2_2 = (float)(PIO2_D - (double)PO2_1);
+constexpr float PO2_3 = (float)(PIO2_D - (double)PO2_1 - (double)PO2_2);
+constexpr float TWO_OVER_PI = (float)(1.0 / PIO2_D);
+__device__ __forceinline__ void sincos_pair(float hi, float lo, float* sn, float* cs) {
+  float q = rintf(hi * TWO_OVER_PI);
+  float r = __fmaf_rn(-q, PO2_1, hi);
+  r = __fmaf_rn(-q, PO2_2, r);
+  r = __fadd_rn(r, __fmaf_rn(-q, PO2_3, lo));
+  const int quad = ((int)q) & 3;
+  const float r2 = r * r;
+  float ps = __fmaf_rn(r2, (float)(1.0 / 362880), (float)(-1.0 / 5040));
+  ps = __fmaf_rn(r2, ps, (float)(1.0 / 120));
+  ps = __fmaf_rn(r2, ps, (float)(-1.0 / 6));
+  ps = __fmaf_rn(r * r2, ps, r);
+  float pc = __fmaf_rn(r2, (float)(-1.0 / 3628800), (float)(1.0 / 40320));
+  pc = __fmaf_rn(r2, pc, (float)(-1.0 / 720));
+  pc = __fmaf_rn(r2, pc, (float)(1.0 / 24));
+  pc = __fmaf_rn(r2, pc, -0.5f);
+  pc = __fmaf_rn(r2, pc, 1.0f);
+  const float a = (quad & 1) ? pc : ps;
+  const float b = (quad & 1) ? ps : pc;
+  *sn = (quad & 2) ? -a : a;
+  *cs = ((quad + 1) & 2) ? -b : b;
+}
+
 // ------------------------------------------------------------------ Philox4x32-10
 // Salmon et al. (SC'11).  Stream element q: block q/4 (128-bit counter), word q%4,
 // key = the seed widened like an int passed to curand_init (kuramoto.cu:57-60).
@@ -168,7 +199,7 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   int pw = pw_of(coup, kmax);
   int o = 0;
   off[0] = o; o += align16(bmax * (int)sizeof(TrajG));
-  off[1] = o; o += align16(bmax * (int)sizeof(SrcB));
+  off[1] = o; o += align16(7 * bmax * (int)sizeof(SrcB));  // [0]: current source; [1..6]: stages 2..7
   off[2] = o; o += align16(KW * bmax * pw * 4);          // red
   off[3] = o; o += align16(bmax * pw * 4);               // rsum
   int sl = KT > bmax * pw ? KT : bmax * pw;
@@ -176,9 +207,48 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[5] = o; o += align16(16 * 4);                      // flags
   off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
   off[7] = o; o += align16(coup == KURA_COUPLING_DENSE ? bmax * CT * 8 : 0); // x tile
-  off[8] = o; o += align16(bmax * 2 * kmax * 4);         // f3 (volcano)
+  // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
+  off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
   off[9] = o; o += align16(coup == KURA_COUPLING_VOLCANO && xs_smem ? bmax * rows * 8 : 0);  // own (cos, sin)
   *total = o;
+}
+
+// Warp reduce-scatter of 16 values per lane: four butterfly levels each halve the
+// values a lane keeps (8 + 4 + 2 + 1 shuffles), a fifth adds the pair.  Afterwards
+// lane l holds, in v[0], the warp total of value index
+// 8*bit4(l) + 4*bit3(l) + 2*bit2(l) + bit1(l) (lanes l and l^1 hold the same total).
+__device__ __forceinline__ void warp_reduce_scatter16(float (&v)[16], int lane) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const bool up = lane & 16;
+    float send = up ? v[j] : v[j + 8];
+    float keep = up ? v[j + 8] : v[j];
+    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const bool up = lane & 8;
+    float send = up ? v[j] : v[j + 4];
+    float keep = up ? v[j + 4] : v[j];
+    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const bool up = lane & 4;
+    float send = up ? v[j] : v[j + 2];
+    float keep = up ? v[j + 2] : v[j];
+    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  {
+    const bool up = lane & 2;
+    float send = up ? v[0] : v[1];
+    float keep = up ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+__device__ __forceinline__ int scatter16_index(int lane) {
+  return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
 }
 
 template <int COUP, int BMAX, int KMAX>
@@ -188,7 +258,8 @@ struct Engine {
 
   const KParams& p;
   TrajG* tr;
-  SrcB* sb;
+  SrcB* sb;       // the source the next coupling evaluation integrates
+  SrcB* sb_base;  // [0]: general source; [1..6]: the six stages of the current attempt
   float* red;
   float* rsum;
   float* slice;
@@ -205,7 +276,8 @@ struct Engine {
     int off[10], total;
     smem_layout(COUP, BMAX, KMAX, pp.rows, pp.xs_smem, off, &total);
     tr = (TrajG*)(smem + off[0]);
-    sb = (SrcB*)(smem + off[1]);
+    sb_base = (SrcB*)(smem + off[1]);
+    sb = sb_base;
     red = (float*)(smem + off[2]);
     rsum = (float*)(smem + off[3]);
     slice = (float*)(smem + off[4]);
@@ -230,6 +302,24 @@ struct Engine {
   // (cos, sin) of row i of trajectory b for the volcano coupling (own rows only)
   __device__ __forceinline__ float2* xrow(int b) {
     return xs ? xs + (size_t)b * p.rows - r0 : p.xbuf + (size_t)b * p.ld;
+  }
+
+  // Thread-to-work mapping of the elementwise phases.  With few rows per CTA (latency
+  // bound) each trajectory of the batch gets its own group of KW/B warps, so the
+  // trajectories proceed side by side; with many rows (throughput bound) all warps
+  // sweep one trajectory after the other.  Returns the trajectory range [b0, b1) of
+  // this thread and its row offset / stride.
+  __device__ __forceinline__ bool all_warps_mode() const { return r1 - r0 >= 1024; }
+  __device__ __forceinline__ void work_map(int& b0, int& b1, int& lt, int& gt) const {
+    if (all_warps_mode()) {
+      b0 = 0; b1 = B; lt = tid; gt = KT;
+    } else {
+      const int nwb = KW / B;
+      b0 = warp / nwb;
+      b1 = b0 < B ? b0 + 1 : b0;
+      lt = (warp - b0 * nwb) * 32 + lane;
+      gt = nwb * 32;
+    }
   }
 
   // Grid barrier with a time limit.  Returns false (on every thread) when the
@@ -271,11 +361,13 @@ struct Engine {
   __device__ void publish_partials(int npw) {
     __syncthreads();
     int par = nbar & 1;
+    const int nwb = KW / B;
+    const bool allw = all_warps_mode();
     for (int v = tid; v < B * npw; v += KT) {
       int b = v / npw, w = v - b * npw;
       float s = 0.f;
-#pragma unroll
-      for (int q = 0; q < KW; ++q) s += red[(q * BMAX + b) * PW + w];
+      const int q0 = allw ? 0 : b * nwb, q1 = allw ? KW : (b + 1) * nwb;
+      for (int q = q0; q < q1; ++q) s += red[(q * BMAX + b) * PW + w];
       p.part[((size_t)(par * G + gi) * B + b) * PW_MAX + w] = s;
     }
   }
@@ -285,7 +377,9 @@ struct Engine {
   __device__ void gather_partials(int npw) {
     const int par = (nbar - 1) & 1;  // the parity published before the barrier just passed
     const int NV = B * npw;
-    int S = KT / NV;
+    // the slicing does not depend on the batch size, so a trajectory's sums (and so its
+    // whole integration) are the same bits whether it runs alone or inside a batch
+    int S = KT / (8 * npw);
     if (S < 1) S = 1;
     if (S > G) S = G;
     const size_t stride = (size_t)B * PW_MAX;
@@ -339,35 +433,65 @@ struct Engine {
     const int n = p.n, ld = p.ld, k = p.k;
     const bool need_part = (COUP == KURA_COUPLING_VOLCANO) || want_r;
     const int npw = (COUP == KURA_COUPLING_VOLCANO ? 2 * k : 0) + (want_r ? 2 : 0);
-    // phase A: stage value, sincos, exchange data and partial sums
-    for (int b = 0; b < B; ++b) {
+    // phase A: stage value, sincos, exchange data and partial sums.  Each trajectory has its
+    // own group of KW/B warps, so the trajectories of a batch proceed side by side.
+    int b0, b1, lt, gt;
+    work_map(b0, b1, lt, gt);
+    for (int b = b0; b < b1; ++b) {
       const SrcB& s = sb[b];
       float acc[PW];
 #pragma unroll
       for (int v = 0; v < PW; ++v) acc[v] = 0.f;
       if (s.active) {
-        const float* hiB = p.ph_hi + ((size_t)s.base * B + b) * ld;
-        const float* loB = p.ph_lo + ((size_t)s.base * B + b) * ld;
+        const size_t boff = ((size_t)s.base * B + b) * ld;
+        const float* hiB = p.ph_hi + boff;
+        const float* loB = p.ph_lo + boff;
         float2* xo = (COUP == KURA_COUPLING_VOLCANO) ? xrow(b) : p.xbuf + ((size_t)xpar * B + b) * ld;
+        const float* gp[7];
+        float Wr[7];
+#pragma unroll
+        for (int j = 0; j < 7; ++j) {
+          gp[j] = p.g + ((size_t)s.slot[j] * B + b) * ld;
+          Wr[j] = s.W[j];
+        }
+        const int nW = s.nW;
+        const float mh = s.m_hi, ml = s.m_lo;
         const bool keep_y7 = s.store_y7;
         const bool emit = s.rec && ((p.dense_level >= 1 && p.mode == MODE_INTEGRATE) || p.mode == MODE_FINAL);
-#pragma unroll 2
-        for (int i = r0 + tid; i < r1; i += KT) {
-          float om = p.omega[i];
-          float gsum = 0.f;
-          for (int j = 0; j < s.nW; ++j) gsum = __fmaf_rn(s.W[j], p.g[((size_t)s.slot[j] * B + b) * ld + i], gsum);
-          f2 pr = two_prod(om, s.m_hi);
-          float pl = om * s.m_lo;
-          f2 s1 = two_sum(hiB[i], pr.hi);
-          f2 s2 = two_sum(s1.hi, gsum);
-          float lo = loB[i] + ((s1.lo + s2.lo) + (pr.lo + pl));
-          float arg = reduce_arg(s2.hi, lo);
+        // U rows per thread and pass: all loads of the U rows are issued before any of
+        // their arithmetic, so their L2 latencies overlap (stores below could alias the
+        // next rows' loads otherwise, which keeps the compiler from hoisting them)
+        constexpr int U = 4;
+        for (int i0 = r0 + lt; i0 < r1; i0 += U * gt) {
+          float om[U], yh[U], yl[U], gsum[U];
+          uint32_t ub[U];
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * gt;
+            const bool ok = i < r1;
+            om[q] = ok ? p.omega[i] : 0.f;
+            yh[q] = ok ? hiB[i] : 0.f;
+            yl[q] = ok ? loB[i] : 0.f;
+            ub[q] = (COUP == KURA_COUPLING_VOLCANO && ok) ? ubits[i - r0] : 0u;
+            gsum[q] = 0.f;
+#pragma unroll
+            for (int j = 0; j < 7; ++j)
+              if (j < nW) gsum[q] = __fmaf_rn(Wr[j], ok ? gp[j][i] : 0.f, gsum[q]);
+          }
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+          const int i = i0 + q * gt;
+          if (i >= r1) break;
+          const f2 pr = two_prod(om[q], mh);
+          const f2 s1 = two_sum(yh[q], pr.hi);
+          const f2 s2 = two_sum(s1.hi, gsum[q]);
+          const float lo = yl[q] + ((s1.lo + s2.lo) + __fmaf_rn(om[q], ml, pr.lo));
           float sn, cs;
-          sincosf(arg, &sn, &cs);
+          sincos_pair(s2.hi, lo, &sn, &cs);
           xo[i] = make_float2(cs, sn);
           if (keep_y7 || emit) {
             f2 y = two_sum(s2.hi, lo);
-            long long w = p.ph_w[((size_t)s.base * B + b) * ld + i];
+            long long w = p.ph_w[boff + i];
             if (keep_y7) {
               float hi7 = y.hi, lo7 = y.lo;
               long long w7 = w;
@@ -385,13 +509,15 @@ struct Engine {
             }
           }
           if (COUP == KURA_COUPLING_VOLCANO) {
-            uint32_t u = ubits[i - r0];
+            // u_m = -1 flips the sign bit: sum_n u_mn (cos_n, sin_n)
+            const uint32_t nu = ~ub[q];
+            const uint32_t cb = __float_as_uint(cs), sbits = __float_as_uint(sn);
 #pragma unroll
             for (int m = 0; m < KMAX; ++m) {
               if (m < k) {
-                float sg = ((u >> m) & 1u) ? 1.f : -1.f;
-                acc[2 * m] = __fmaf_rn(sg, cs, acc[2 * m]);
-                acc[2 * m + 1] = __fmaf_rn(sg, sn, acc[2 * m + 1]);
+                const uint32_t sg = (nu << (31 - m)) & 0x80000000u;
+                acc[2 * m] += __uint_as_float(cb ^ sg);
+                acc[2 * m + 1] += __uint_as_float(sbits ^ sg);
               }
             }
           }
@@ -399,18 +525,22 @@ struct Engine {
             acc[PW - 2] += cs;
             acc[PW - 1] += sn;
           }
+          }
         }
       }
       if (need_part) {
         // compact layout: [2k projections][sum cos, sum sin]
         float* dst = red + (warp * BMAX + b) * PW;
         if (COUP == KURA_COUPLING_VOLCANO) {
+          // the 2*KMAX projections, 16 at a time, reduce-scattered across the warp
 #pragma unroll
-          for (int v = 0; v < 2 * KMAX; ++v) {
-            if (v < 2 * k) {
-              float t = warp_sum(acc[v]);
-              if (lane == 0) dst[v] = t;
-            }
+          for (int c0 = 0; c0 < 2 * KMAX; c0 += 16) {
+            float v16[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v16[j] = acc[c0 + j];
+            warp_reduce_scatter16(v16, lane);
+            const int v = c0 + scatter16_index(lane);
+            if (!(lane & 1) && v < 2 * k) dst[v] = v16[0];
           }
         }
         if (want_r) {
@@ -437,25 +567,56 @@ struct Engine {
         f3[v] = (m < k) ? (sgn * rsum[b * PW + w]) / (float)n : 0.f;
       }
       __syncthreads();
-      for (int b = 0; b < B; ++b) {
-        if (!sb[b].active) continue;
+      // m2 (kuramoto.cu:83-101): F_n = sum_m u_mn f3_m, summed in order of m.  For k <= 8
+      // the 2^k sums, one per sign pattern, are tabulated once and looked up per row.
+      float2* tab = reinterpret_cast<float2*>(f3 + BMAX * 2 * KMAX);
+      const bool use_tab = (k <= 8);
+      if (use_tab) {
+        for (int v = tid; v < (B << k); v += KT) {
+          const int b = v >> k, pat = v & ((1 << k) - 1);
+          const float* fb = f3 + b * 2 * KMAX;
+          float Fc = 0.f, Fs = 0.f;
+          for (int m = 0; m < k; ++m) {
+            const bool pos = (pat >> m) & 1;
+            Fc += pos ? fb[2 * m] : -fb[2 * m];
+            Fs += pos ? fb[2 * m + 1] : -fb[2 * m + 1];
+          }
+          tab[b * 256 + pat] = make_float2(Fc, Fs);
+        }
+        __syncthreads();
+      }
+      for (int b = b0; b < b1; ++b) {
+        const SrcB& s = sb[b];
+        if (!s.active) continue;
         const float2* xb = xrow(b);
         const float* fb = f3 + b * 2 * KMAX;
-#pragma unroll 2
-        for (int i = r0 + tid; i < r1; i += KT) {
-          uint32_t u = ubits[i - r0];
+        const float2* tb = tab + b * 256;
+        const float c1 = tr[b].c1;
+        float* gdst = s.gout >= 0 ? p.g + ((size_t)s.gout * B + b) * ld : nullptr;
+        const bool rec = s.rec;
+        for (int i = r0 + lt; i < r1; i += gt) {
+          const uint32_t u = ubits[i - r0];
           float Fc = 0.f, Fs = 0.f;
-          // m2 (kuramoto.cu:83-101): F_n = sum_m u_mn f3_m, sequential in m
+          if (use_tab) {
+            const float2 F = tb[u];
+            Fc = F.x;
+            Fs = F.y;
+          } else {
 #pragma unroll
-          for (int m = 0; m < KMAX; ++m) {
-            if (m < k) {
-              bool pos = (u >> m) & 1u;
-              Fc += pos ? fb[2 * m] : -fb[2 * m];
-              Fs += pos ? fb[2 * m + 1] : -fb[2 * m + 1];
+            for (int m = 0; m < KMAX; ++m) {
+              if (m < k) {
+                bool pos = (u >> m) & 1u;
+                Fc += pos ? fb[2 * m] : -fb[2 * m];
+                Fs += pos ? fb[2 * m + 1] : -fb[2 * m + 1];
+              }
             }
           }
-          float2 x = xb[i];
-          epilogue(b, i, Fc, Fs, x.x, x.y);
+          const float2 x = xb[i];
+          if (!rec && gdst) {
+            gdst[i] = c1 * (x.y * Fc - x.x * Fs);
+          } else {
+            epilogue(b, i, Fc, Fs, x.x, x.y);
+          }
         }
       }
     } else {
@@ -488,7 +649,8 @@ struct Engine {
       for (int q = 0; q < RG; ++q)
 #pragma unroll
         for (int b = 0; b < BMAX; ++b) acc[q][b][0] = acc[q][b][1] = 0.f;
-      const int row0 = pr0 + warp * RG;
+      // warp w takes rows pr0 + w + KW*q of the pass, so small row blocks keep every warp busy
+      const int row0 = pr0 + warp;
       for (int c0 = 0; c0 < ld; c0 += CT) {
         __syncthreads();
         const int cw = min(CT, ld - c0);
@@ -501,7 +663,7 @@ struct Engine {
           float4 a[RG];
 #pragma unroll
           for (int q = 0; q < RG; ++q) {
-            int row = row0 + q;
+            int row = row0 + KW * q;
             a[q] = (row < r1) ? ld_stream4(p.adj + (size_t)row * ld + c0 + cc) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
 #pragma unroll
@@ -530,7 +692,7 @@ struct Engine {
       for (int q = 0; q < RG; ++q)
 #pragma unroll
         for (int b = 0; b < BMAX; ++b) {
-          int row = row0 + q;
+          int row = row0 + KW * q;
           if (lane == q * BMAX + b && b < B && row < r1 && sb[b].active) {
             float2 x = __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + row]);
             epilogue(b, row, acc[q][b][0], acc[q][b][1], x.x, x.y);
@@ -542,15 +704,37 @@ struct Engine {
   // ---- error norm of the attempt (dp45.cu:79-84, 116-119); sum of squares -> rsum[b*PW]
   __device__ bool error_phase() {
     const int ld = p.ld;
-    for (int b = 0; b < B; ++b) {
+    int b0, b1, lt, gt;
+    work_map(b0, b1, lt, gt);
+    for (int b = b0; b < b1; ++b) {
       const SrcB& s = sb[b];
       float acc = 0.f;
       if (s.active) {
         const size_t yb = ((size_t)s.base * B + b) * ld, y7b = ((size_t)(s.base ^ 1) * B + b) * ld;
-        for (int i = r0 + tid; i < r1; i += KT) {
-          float e = 0.f;
+        const float* gp[7];
+        float Er[7];
 #pragma unroll
-          for (int j = 0; j < 7; ++j) e = __fmaf_rn(s.E[j], p.g[((size_t)s.slot[j] * B + b) * ld + i], e);
+        for (int j = 0; j < 7; ++j) {
+          gp[j] = p.g + ((size_t)s.slot[j] * B + b) * ld;
+          Er[j] = s.E[j];
+        }
+        constexpr int U = 4;
+        for (int i0 = r0 + lt; i0 < r1; i0 += U * gt) {
+          float ev[U];
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+            const int i = i0 + q * gt;
+            ev[q] = 0.f;
+            if (i < r1) {
+#pragma unroll
+              for (int j = 0; j < 7; ++j) ev[q] = __fmaf_rn(Er[j], gp[j][i], ev[q]);
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < U; ++q) {
+          const int i = i0 + q * gt;
+          if (i >= r1) break;
+          float e = ev[q];
           float tol = (float)p.atol;
           if (p.rtol != 0.0) {
             float a0 = fabsf(__fmaf_rn((float)p.ph_w[yb + i], P2_1, p.ph_hi[yb + i]));
@@ -559,6 +743,7 @@ struct Engine {
           }
           float ye = e / tol;
           acc = __fmaf_rn(ye, ye, acc);
+          }
         }
       }
       float t = warp_sum(acc);
@@ -570,12 +755,14 @@ struct Engine {
     return true;
   }
 
-  // ---- per-trajectory sources, filled by 16 threads per trajectory
-  // stage s of the attempt (the stage loop of dp45_step, dp45.cu:90-106)
-  __device__ void setup_stage(int s) {
-    if (tid < B * 16) {
-      const int b = tid >> 4, j = tid & 15;
-      SrcB& S = sb[b];
+  // ---- per-trajectory sources
+  // the six stages of one attempt (the stage loop of dp45_step, dp45.cu:90-106), filled at
+  // once by 16 threads per (stage, trajectory); the active flags are copied from sb_base
+  __device__ void setup_attempt() {
+    __syncthreads();  // the active flags were just written by threads tid < B
+    for (int t = tid; t < 6 * B * 16; t += KT) {
+      const int j = t & 15, b = (t >> 4) % B, s = 2 + (t >> 4) / B;
+      SrcB& S = sb_base[(s - 1) * BMAX + b];
       const TrajG& T = tr[b];
       const double h = T.h;
       if (j < 7) {
@@ -598,6 +785,7 @@ struct Engine {
         S.rec = 0;
         S.oslot = -1;
         S.oidx = 0;
+        S.active = sb_base[b].active;
       }
     }
     __syncthreads();
@@ -659,7 +847,8 @@ struct Engine {
         T.status = KURA_ERR_NONFINITE;
         return;
       }
-      factor = 0.9 * pow(norm, -0.2);  // norm = +inf gives 0: the attempt is rejected with the 0.2 floor
+      // 0.9 norm^(-1/5) (dp45.cu:120); norm = +inf gives 0: the attempt is rejected with the 0.2 floor
+      factor = (double)(0.9f * exp2f(-0.2f * log2f((float)norm)));
       accept = norm < 1.0;
     }
     if (accept) {
@@ -814,15 +1003,18 @@ struct Engine {
         sb[tid].active = (T.status == 0 && T.eval_i >= T.eval_end && T.t < T.t1 &&
                           !(p.log_cap > 0 && T.log_count >= p.log_cap));
       }
+      setup_attempt();  // ends with __syncthreads
       for (int s = 2; s <= 7; ++s) {
-        setup_stage(s);  // ends with __syncthreads
+        sb = sb_base + (s - 1) * BMAX;
         if (!coupling_eval(false)) return;
       }
+      // sb stays on stage 7: the error phase uses its E weights, slots and phase buffers
       if (!p.fixed) {
         if (!error_phase()) return;
       }
       if (tid < B && sb[tid].active) decide(tid);
       __syncthreads();
+      sb = sb_base;
       attempts++;
     }
     write_back();
