@@ -40,9 +40,17 @@ WORKLOADS = {
     # the reference's default dense case (configs: N=5000, K=5, c=3, Cauchy, theta0=0, t=100, dt=1)
     "dense5000": dict(n=5000, k=5, coupling=0, cs=[3.0], normal=False, init=0.0, t1=100.0, dt=1.0, atol=1e-6,
                       rtol=0.0, shared_theta=True),
-    # the plain FP32 path at N=65536: 8 trajectories per pass over A, bounded horizon
-    "dense65536": dict(n=65536, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.5, dt=0.1,
+    # the plain FP32 path at N=65536 (17.2 GB adjacency read once per RHS; x8: shared by 8
+    # trajectories of one pass), Cauchy omega, theta0 uniform in [0, 2pi); the Cauchy
+    # outliers of N=65536 force steps of ~1e-4, so the horizon is short
+    "dense65536": dict(n=65536, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
                        atol=1e-6, rtol=0.0, shared_theta=False),
+    "dense65536x8": dict(n=65536, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.004,
+                         dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False),
+    "dense16384": dict(n=16384, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
+                       atol=1e-6, rtol=0.0, shared_theta=False),
+    "dense16384x8": dict(n=16384, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.004,
+                         dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False),
 }
 # algorithmic bytes per accepted oscillator-step of the dominant kernel
 #   volcano: the DP45 state a step moves in the reference design (~150 B)

@@ -254,7 +254,8 @@ __device__ __forceinline__ int scatter16_index(int lane) {
 template <int COUP, int BMAX, int KMAX>
 struct Engine {
   static constexpr int PW = pw_of(COUP, KMAX);
-  static constexpr int RG = BMAX == 1 ? 4 : (BMAX == 2 ? 2 : 1);
+  // rows per warp and pass of the dense coupling: each staged x value is reused RG times
+  static constexpr int RG = BMAX == 1 ? 4 : (BMAX == 2 ? 4 : 4);
 
   const KParams& p;
   TrajG* tr;
@@ -553,12 +554,21 @@ struct Engine {
         }
       }
     }
+    // phase C is needed when a slope or coupling output is written; an output pass that
+    // records only r skips it
+    bool need_F = false;
+    for (int bb = 0; bb < B; ++bb) {
+      const SrcB& sbb = sb[bb];
+      need_F |= sbb.active && (sbb.gout >= 0 || (sbb.rec && (p.dense_level >= 2 || p.mode != MODE_INTEGRATE)));
+    }
     if (need_part) publish_partials(npw);
     if (!grid_sync()) return false;
     if (need_part) gather_partials(npw);
 
     // phase C: couplings for the CTA's rows
-    if (COUP == KURA_COUPLING_VOLCANO) {
+    if (!need_F) {
+      // r only
+    } else if (COUP == KURA_COUPLING_VOLCANO) {
       // f3[b][2m] = (-1)^m / N * sum_n u_mn cos_n (m1, kuramoto.cu:62-81)
       for (int v = tid; v < B * 2 * KMAX; v += KT) {
         int b = v / (2 * KMAX), w = v % (2 * KMAX);
