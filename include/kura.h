@@ -36,6 +36,15 @@ extern "C" {
 #define KURA_COUPLING_DENSE 0   /* adjacency stored in HBM (reference default) */
 #define KURA_COUPLING_VOLCANO 1 /* rank-K volcano factor regenerated from Philox (reference -A) */
 
+/* KURA_ENGINE_AUTO picks the tensor-core ensemble for a dense network with batch > 8 and
+ * the CUDA-core persistent kernel otherwise.  The persistent kernel takes batch <= 8 (dense
+ * or volcano coupling, every dense level); the tensor-core ensemble takes a dense network
+ * with batch <= 128, keeps only the order parameter (dense level 0) and reports no per-step
+ * records.  The reference has neither: it integrates one trajectory per process. */
+#define KURA_ENGINE_AUTO 0
+#define KURA_ENGINE_PERSISTENT 1
+#define KURA_ENGINE_TENSOR 2
+
 typedef struct kura_handle kura_handle;
 
 /* Network and integrator settings; the reference flag each field replaces is given. */
@@ -50,7 +59,7 @@ typedef struct kura_config {
   int32_t fixed_step;  /* -F */
   int32_t device;      /* -g */
   int32_t dense_level; /* -D: 0 order only; >=1 adds phases and step times; >=2 adds couplings */
-  int32_t reserved0;
+  int32_t engine;      /* KURA_ENGINE_*: which kernels integrate the batch */
   void* stream;        /* cudaStream_t for every launch and copy (NULL: a stream owned by the handle) */
 } kura_config;
 

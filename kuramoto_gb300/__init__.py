@@ -15,7 +15,10 @@ from .native import (  # noqa: F401
     volcano_factor,
     COUPLING_DENSE,
     COUPLING_VOLCANO,
+    ENGINE_AUTO,
+    ENGINE_PERSISTENT,
+    ENGINE_TENSOR,
 )
 
 __all__ = ["KuraError", "Network", "lib", "lib_path", "cli_path", "random_inputs", "volcano_factor",
-           "COUPLING_DENSE", "COUPLING_VOLCANO"]
+           "COUPLING_DENSE", "COUPLING_VOLCANO", "ENGINE_AUTO", "ENGINE_PERSISTENT", "ENGINE_TENSOR"]

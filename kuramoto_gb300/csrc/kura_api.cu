@@ -15,6 +15,7 @@
 #include <vector>
 #include "kura.h"
 #include "kura_kernels.cuh"
+#include "kura_tensor.h"
 
 using kura::TrajG;
 
@@ -72,7 +73,15 @@ struct kura_handle {
   bool omega_set = false, adj_set = false, horizon_set = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   kura_stats stats{};
+  kura::TensorEngine* te = nullptr;  // the tensor-core ensemble, when selected
 };
+
+// KURA_ENGINE_AUTO: tensor cores for a dense network with more than 8 trajectories
+static int resolve_engine(const kura_config* c) {
+  if (c->engine == KURA_ENGINE_TENSOR) return KURA_ENGINE_TENSOR;
+  if (c->engine == KURA_ENGINE_PERSISTENT) return KURA_ENGINE_PERSISTENT;
+  return (c->coupling == KURA_COUPLING_DENSE && c->batch > 8) ? KURA_ENGINE_TENSOR : KURA_ENGINE_PERSISTENT;
+}
 
 extern "C" const char* kura_last_error(void) { return g_err.c_str(); }
 void kura::set_last_error(const char* msg) { g_err = msg; }
@@ -89,7 +98,16 @@ static int validate(const kura_config* c) {
   if (!c) return fail(KURA_ERR_INVALID, "config is NULL");
   if (c->n < 1 || c->n > (1LL << 30)) return fail(KURA_ERR_INVALID, "n must be in [1, 2^30]");
   if (c->batch < 1) return fail(KURA_ERR_INVALID, "batch must be >= 1");
-  if (c->batch > 8) return fail(KURA_ERR_UNSUPPORTED, "batch > 8 is not built into the persistent kernel");
+  if (c->engine < 0 || c->engine > 2) return fail(KURA_ERR_INVALID, "unknown engine");
+  if (resolve_engine(c) == KURA_ENGINE_TENSOR) {
+    if (c->coupling != KURA_COUPLING_DENSE)
+      return fail(KURA_ERR_UNSUPPORTED, "the tensor-core ensemble needs a dense adjacency");
+    if (c->batch > 128) return fail(KURA_ERR_UNSUPPORTED, "the tensor-core ensemble takes batch <= 128");
+    if (c->dense_level != 0)
+      return fail(KURA_ERR_UNSUPPORTED, "the tensor-core ensemble keeps the order parameter only (dense level 0)");
+  } else if (c->batch > 8) {
+    return fail(KURA_ERR_UNSUPPORTED, "batch > 8 needs a dense network on the tensor-core ensemble");
+  }
   if (c->k < 0) return fail(KURA_ERR_INVALID, "k must be >= 0");
   if (c->coupling != KURA_COUPLING_DENSE && c->coupling != KURA_COUPLING_VOLCANO)
     return fail(KURA_ERR_INVALID, "unknown coupling");
@@ -105,6 +123,10 @@ static int validate(const kura_config* c) {
 extern "C" int kura_memory_required(const kura_config* c, int64_t* bytes) {
   int rc = validate(c);
   if (rc) return rc;
+  if (resolve_engine(c) == KURA_ENGINE_TENSOR) {
+    *bytes = (int64_t)kura::TensorEngine::memory_required(c->n, c->batch);
+    return KURA_OK;
+  }
   int ld, bmax, kmax;
   plan(c, &ld, &bmax, &kmax);
   long long B = c->batch, n = ld;
@@ -128,6 +150,7 @@ extern "C" void kura_destroy(kura_handle* h) {
     if (p) cudaFree(p);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  delete h->te;
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -173,6 +196,21 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   }
   CUH(cudaEventCreate(&h->ev0));
   CUH(cudaEventCreate(&h->ev1));
+  h->htraj.assign(h->B, TrajG{});
+  for (auto& T : h->htraj) T.status = 1;  // no state yet
+  h->c1.assign(h->B, 0.f);
+  h->t0.assign(h->B, 0.0);
+  h->order.assign(h->B, {});
+  if (resolve_engine(cfg) == KURA_ENGINE_TENSOR) {
+    h->te = new kura::TensorEngine();
+    int rc2 = h->te->init(cfg->n, cfg->k, cfg->batch, cfg->seed, cfg->atol, cfg->rtol, cfg->fixed_step,
+                          cfg->dense_level, cfg->device, h->stream);
+    if (rc2) return bail(fail(rc2, kura::TensorEngine::last_error()));
+    h->stats.grid = 0;
+    h->stats.block = 160;
+    *out = h;
+    return KURA_OK;
+  }
 
   // grid: one or more CTAs per SM, all co-resident (cooperative launch)
   int dev = cfg->device, sms = 0, coop = 0;
@@ -238,6 +276,12 @@ extern "C" int kura_set_frequencies(kura_handle* h, const float* omega, int64_t 
   if (!h || !omega) return fail(KURA_ERR_INVALID, "NULL argument");
   if (n != h->n) return fail(KURA_ERR_INVALID, "frequency count differs from n");
   CU(cudaSetDevice(h->cfg.device));
+  if (h->te) {
+    int rc = h->te->set_frequencies(omega);
+    if (rc) return fail(rc, kura::TensorEngine::last_error());
+    h->omega_set = true;
+    return KURA_OK;
+  }
   CU(cudaMemcpyAsync(h->omega, omega, sizeof(float) * n, cudaMemcpyHostToDevice, h->stream));
   CU(cudaStreamSynchronize(h->stream));
   h->omega_set = true;
@@ -249,6 +293,12 @@ extern "C" int kura_set_adjacency(kura_handle* h, const float* adj, int64_t n) {
   if (h->coupling != KURA_COUPLING_DENSE) return fail(KURA_ERR_INVALID, "adjacency is regenerated (volcano coupling)");
   if (n != h->n) return fail(KURA_ERR_INVALID, "adjacency size differs from n");
   CU(cudaSetDevice(h->cfg.device));
+  if (h->te) {
+    int rc = h->te->set_adjacency(adj);
+    if (rc) return fail(rc, kura::TensorEngine::last_error());
+    h->adj_set = true;
+    return KURA_OK;
+  }
   CU(cudaMemcpy2DAsync(h->adj, sizeof(float) * h->ld, adj, sizeof(float) * n, sizeof(float) * n, n,
                        cudaMemcpyHostToDevice, h->stream));
   CU(cudaStreamSynchronize(h->stream));
@@ -260,6 +310,12 @@ extern "C" int kura_generate_adjacency(kura_handle* h) {
   if (!h) return fail(KURA_ERR_INVALID, "handle is NULL");
   if (h->coupling != KURA_COUPLING_DENSE) return fail(KURA_ERR_INVALID, "adjacency is regenerated (volcano coupling)");
   CU(cudaSetDevice(h->cfg.device));
+  if (h->te) {
+    int rc = h->te->generate_adjacency();
+    if (rc) return fail(rc, kura::TensorEngine::last_error());
+    h->adj_set = true;
+    return KURA_OK;
+  }
   int words = (h->K + 31) / 32;
   uint32_t* bits = nullptr;
   if (words > 0) {
@@ -278,6 +334,10 @@ extern "C" int kura_get_adjacency(kura_handle* h, float* adj, int64_t n) {
   if (h->coupling != KURA_COUPLING_DENSE || !h->adj_set) return fail(KURA_ERR_INVALID, "no stored adjacency");
   if (n != h->n) return fail(KURA_ERR_INVALID, "adjacency size differs from n");
   CU(cudaSetDevice(h->cfg.device));
+  if (h->te) {
+    int rc = h->te->get_adjacency(adj);
+    return rc ? fail(rc, kura::TensorEngine::last_error()) : KURA_OK;
+  }
   CU(cudaMemcpy2DAsync(adj, sizeof(float) * n, h->adj, sizeof(float) * h->ld, sizeof(float) * n, n,
                        cudaMemcpyDeviceToHost, h->stream));
   CU(cudaStreamSynchronize(h->stream));
@@ -293,9 +353,11 @@ extern "C" int kura_set_coupling(kura_handle* h, int32_t traj, float c) {
 }
 
 static int set_state_common(kura_handle* h, int traj, const float* dev_theta, double t, double step) {
-  size_t off = (size_t)traj * h->ld;  // physical buffer 0
-  CU(kura::launch_init_state(dev_theta, h->n, h->ld, h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->stream));
-  CU(cudaStreamSynchronize(h->stream));
+  if (!h->te) {
+    size_t off = (size_t)traj * h->ld;  // physical buffer 0
+    CU(kura::launch_init_state(dev_theta, h->n, h->ld, h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+  }
   TrajG& T = h->htraj[traj];
   float c = T.c1;
   T = TrajG{};
@@ -308,6 +370,10 @@ static int set_state_common(kura_handle* h, int traj, const float* dev_theta, do
   T.need_k1 = 1;
   T.need_init = 0;
   h->horizon_set = false;
+  if (h->te) {
+    int rc = h->te->set_state(traj, dev_theta, T);
+    if (rc) return fail(rc, kura::TensorEngine::last_error());
+  }
   return KURA_OK;
 }
 
@@ -317,7 +383,7 @@ extern "C" int kura_set_state(kura_handle* h, int32_t traj, const float* theta, 
   if (!theta) return fail(KURA_ERR_INVALID, "theta is NULL");
   if (!(step > 0)) return fail(KURA_ERR_INVALID, "step must be > 0");
   CU(cudaSetDevice(h->cfg.device));
-  float* tmp = h->fin_theta + (size_t)traj * h->ld;
+  float* tmp = h->te ? h->te->staging(traj) : h->fin_theta + (size_t)traj * h->ld;
   CU(cudaMemcpyAsync(tmp, theta, sizeof(float) * h->n, cudaMemcpyHostToDevice, h->stream));
   return set_state_common(h, traj, tmp, t, step);
 }
@@ -349,6 +415,24 @@ extern "C" int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t in
   h->n_eval = (int)h->t_eval_h.size();
   h->dt = dt;
   h->t1 = t1;
+  if (h->te) {
+    for (int b = 0; b < h->B; ++b) {
+      TrajG& T = h->htraj[b];
+      T.t1 = t1;
+      T.eval_i = 0;
+      T.eval_end = 0;
+      T.need_init = initial_record ? 1 : 0;
+      T.out_count = 0;
+      T.log_count = 0;
+      h->order[b].clear();
+      h->t0[b] = T.t;
+    }
+    h->ring = h->n_eval + 2;
+    int rc = h->te->set_horizon(h->t_eval_h, h->ring, h->htraj);
+    if (rc) return fail(rc, kura::TensorEngine::last_error());
+    h->horizon_set = true;
+    return KURA_OK;
+  }
   if (h->n_eval > h->t_eval_alloc || !h->t_eval) {
     if (h->t_eval) cudaFree(h->t_eval);
     h->t_eval = nullptr;
@@ -436,6 +520,44 @@ extern "C" int kura_run(kura_handle* h, const kura_callbacks* cb) {
   if (h->coupling == KURA_COUPLING_DENSE && !h->adj_set) return fail(KURA_ERR_INVALID, "adjacency not set");
   if (!h->horizon_set) return fail(KURA_ERR_INVALID, "horizon not set (kura_set_horizon after kura_set_state)");
   CU(cudaSetDevice(h->cfg.device));
+  if (h->te) {
+    int rc = h->te->run(h->htraj, h->stats);
+    if (rc) return fail(rc, kura::TensorEngine::last_error());
+    long long acc = 0, rej = 0;
+    int errc = 0;
+    std::vector<float> rbuf;
+    std::vector<int> ibuf;
+    for (int b = 0; b < h->B; ++b) {
+      TrajG& T = h->htraj[b];
+      acc += T.accepted;
+      rej += T.rejected;
+      if (T.status < 0 && !errc) errc = T.status;
+      rbuf.resize(std::max(T.out_count, 1));
+      ibuf.resize(std::max(T.out_count, 1));
+      if (T.out_count > 0) {
+        rc = h->te->read_order(b, T.out_count, rbuf.data(), ibuf.data());
+        if (rc) return fail(rc, kura::TensorEngine::last_error());
+      }
+      for (int q = 0; q < T.out_count; ++q) {
+        h->order[b].push_back(rbuf[q]);
+        if (cb && cb->on_output) {
+          const int idx = ibuf[q];
+          const double te = idx < 0 ? h->t0[b] : (double)h->t_eval_h[idx];
+          if (cb->on_output(cb->user, b, idx, te, rbuf[q], nullptr, nullptr))
+            return fail(KURA_ERR_CALLBACK, "on_output aborted");
+        }
+      }
+    }
+    h->stats.accepted = acc;
+    h->stats.rejected = rej;
+    if (errc) {
+      const char* m = errc == KURA_ERR_STEP_UNDERFLOW ? "step size underflow"
+                      : errc == KURA_ERR_UNSUPPORTED ? "more than 32 output times crossed in one step"
+                                                      : "non-finite error norm";
+      return fail(errc, m);
+    }
+    return KURA_OK;
+  }
   const bool log_steps = cb && cb->on_step;
   std::vector<float> rbuf, thbuf, cpbuf;
   std::vector<int> ibuf;
@@ -534,7 +656,10 @@ extern "C" int kura_get_state(kura_handle* h, int32_t traj, float* theta, double
   if (rc) return rc;
   CU(cudaSetDevice(h->cfg.device));
   const TrajG& T = h->htraj[traj];
-  if (theta) {
+  if (theta && h->te) {
+    int rc2 = h->te->get_state(traj, T.rot_y, theta);
+    if (rc2) return fail(rc2, kura::TensorEngine::last_error());
+  } else if (theta) {
     size_t off = ((size_t)T.rot_y * h->B + traj) * h->ld;
     float* tmp = h->fin_theta + (size_t)traj * h->ld;
     CU(kura::launch_unwrap(h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->n, tmp, h->stream));
@@ -561,6 +686,13 @@ extern "C" int kura_final_record(kura_handle* h, int32_t traj, float* theta, flo
   if (rc) return rc;
   if (!h->horizon_set) return fail(KURA_ERR_INVALID, "no run to report");
   CU(cudaSetDevice(h->cfg.device));
+  if (h->te) {
+    rc = h->te->evaluate(1, traj, theta, couplings);
+    if (rc) return fail(rc, kura::TensorEngine::last_error());
+    if (t) *t = h->htraj[traj].t;
+    if (step) *step = h->htraj[traj].h;
+    return KURA_OK;
+  }
   rc = launch(h, kura::MODE_FINAL, false);
   if (rc) return rc;
   if (theta) CU(cudaMemcpy(theta, h->fin_theta + (size_t)traj * h->ld, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
@@ -581,6 +713,10 @@ extern "C" int kura_rhs(kura_handle* h, int32_t traj, const float* theta, float*
   // the batch is evaluated at its current phases; this trajectory is first set to theta
   rc = kura_set_state(h, traj, theta, 0.0, 1.0);
   if (rc) return rc;
+  if (h->te) {
+    rc = h->te->evaluate(2, traj, dtheta, couplings);
+    return rc ? fail(rc, kura::TensorEngine::last_error()) : KURA_OK;
+  }
   rc = launch(h, kura::MODE_RHS, false);
   if (rc) return rc;
   if (dtheta) CU(cudaMemcpy(dtheta, h->fin_theta + (size_t)traj * h->ld, sizeof(float) * h->n, cudaMemcpyDeviceToHost));

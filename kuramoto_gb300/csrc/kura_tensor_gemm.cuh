@@ -1,0 +1,193 @@
+// kura_tensor_gemm.cuh -- tcgen05 GEMM with a fused epilogue:
+//   C[m][c] = sum_k A[m][k] * X[c][k]      (A: M x K BF16, X: NCOL x K BF16, both K-major)
+// accumulated in FP32 in tensor memory.  One CTA computes a 128-row tile times all
+// NCOL columns (NCOL <= 512, the whole TMEM), looping over row tiles (persistent).
+//
+// Roles (160 threads): warp 0 lane 0 streams A and X tiles with TMA into a ring of
+// STAGES shared-memory stages; warp 1 lane 0 issues the MMAs (M = 128, N = min(NCOL,
+// 256), K = 16 per instruction) and commits each stage back to the producer; warps 1-4
+// read the accumulator (warp w owns TMEM lanes 32*(w%4)..+31, one tile row per thread)
+// and call the epilogue.  Every wait is bounded: on a timeout the CTA records an error,
+// stops issuing work, waits (bounded) for its own TMA copies, frees TMEM and returns.
+#pragma once
+#include "kura_umma.cuh"
+
+namespace kura {
+
+constexpr int TG_BM = 128;  // rows per tile (M of one MMA)
+constexpr int TG_BK = 64;   // K per stage (one 128-byte swizzle row of BF16)
+constexpr int TG_THREADS = 160;
+
+template <int NCOL> struct TGCfg {
+  static constexpr int NMMA = NCOL > 256 ? 256 : NCOL;  // N of one MMA instruction
+  static constexpr int NH = NCOL / NMMA;                // MMAs per K step
+  static constexpr int A_BYTES = TG_BM * TG_BK * 2;
+  static constexpr int X_BYTES = NCOL * TG_BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + X_BYTES;
+  static constexpr int STAGES = (200 * 1024) / STAGE_BYTES > 6 ? 6 : (200 * 1024) / STAGE_BYTES;
+  static constexpr int TMEM_COLS = NCOL < 32 ? 32 : NCOL;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
+  static_assert(NCOL % 16 == 0 && NCOL <= 512, "NCOL");
+  static_assert(STAGES >= 2, "stages");
+};
+
+// Epilogue interface: Epi::row(taddr, row, m0) is called by every thread of warps 1-4
+// with taddr = TMEM address of this thread's accumulator row (lane field set, column 0).
+template <int NCOL, class Epi>
+__global__ void __launch_bounds__(TG_THREADS, 1)
+    k_tensor_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int mtiles,
+                  int ktiles, Epi epi, int* err, unsigned long long limit_ns, const int* run_flag) {
+  using C = TGCfg<NCOL>;
+  if (run_flag && *run_flag == 0) return;  // nothing to compute (every column inactive)
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = (uint64_t*)(smem + C::STAGES * C::STAGE_BYTES);
+  uint64_t* full = bars;                    // [STAGES]
+  uint64_t* empty = bars + C::STAGES;       // [STAGES]
+  uint64_t* accfull = bars + 2 * C::STAGES; // MMAs of a tile done
+  uint64_t* accempty = accfull + 1;         // epilogue of a tile done (4 warp arrivals)
+  uint32_t* tmem_slot = (uint32_t*)(accempty + 1);
+  volatile int* sabort = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < C::STAGES; ++s) {
+      umma::mbar_init(&full[s], 1);
+      umma::mbar_init(&empty[s], 1);
+    }
+    umma::mbar_init(accfull, 1);
+    umma::mbar_init(accempty, 4);
+    *sabort = 0;
+    umma::fence_barrier_init();
+    umma::prefetch_tmap(&tmA);
+    umma::prefetch_tmap(&tmX);
+  }
+  if (warp == 2) umma::tmem_alloc(tmem_slot, C::TMEM_COLS);
+  umma::tc_fence_before();
+  __syncthreads();
+  umma::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t idesc = umma::idesc_bf16_f32(TG_BM, C::NMMA);
+
+  if (warp == 0) {
+    // ---------------- TMA producer
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      long long issued = 0, consumed_hint = 0;
+      (void)consumed_hint;
+      for (int tile = blockIdx.x; tile < mtiles && !*sabort; tile += gridDim.x) {
+        for (int kt = 0; kt < ktiles; ++kt) {
+          if (!umma::mbar_wait(&empty[s], ph ^ 1, limit_ns, sabort)) {
+            *sabort = 1;
+            break;
+          }
+          unsigned char* st = smem + s * C::STAGE_BYTES;
+          umma::mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
+          umma::tma_load_2d(st, &tmA, &full[s], kt * TG_BK, tile * TG_BM);
+#pragma unroll
+          for (int h = 0; h < (NCOL + 255) / 256; ++h) {
+            const int rows = NCOL - h * 256 < 256 ? NCOL - h * 256 : 256;
+            (void)rows;
+            umma::tma_load_2d(st + C::A_BYTES + h * 256 * 128, &tmX, &full[s], kt * TG_BK, h * 256);
+          }
+          ++issued;
+          if (++s == C::STAGES) { s = 0; ph ^= 1; }
+        }
+      }
+      // drain: wait (bounded) until every issued stage has landed, so no copy is in
+      // flight when the CTA exits
+      int ds = s;
+      uint32_t dph = ph;
+      for (int q = 0; q < C::STAGES; ++q) {
+        if (--ds < 0) { ds = C::STAGES - 1; dph ^= 1; }
+        if (issued - q <= 0) break;
+        umma::mbar_wait(&full[ds], dph, limit_ns, nullptr);
+      }
+    }
+  } else {
+    // ---------------- MMA issue (warp 1 lane 0) and epilogue (warps 1-4)
+    int s = 0;
+    uint32_t ph = 0;
+    uint32_t it = 0;
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    for (int tile = blockIdx.x; tile < mtiles; tile += gridDim.x, ++it) {
+      if (warp == 1) {
+        if (lane == 0 && !*sabort) {
+          // the accumulator must have been read out by the previous tile's epilogue
+          if (!umma::mbar_wait(accempty, (it & 1) ^ 1, limit_ns, sabort)) *sabort = 1;
+          umma::tc_fence_after();
+          for (int kt = 0; kt < ktiles && !*sabort; ++kt) {
+            if (!umma::mbar_wait(&full[s], ph, limit_ns, sabort)) {
+              *sabort = 1;
+              break;
+            }
+            umma::tc_fence_after();
+            const uint32_t a0 = umma::smem_u32(smem + s * C::STAGE_BYTES);
+            const uint32_t x0 = a0 + C::A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TG_BK / 16; ++kk) {
+              const uint64_t ad = umma::sw128_desc(a0 + kk * 32);
+#pragma unroll
+              for (int h = 0; h < C::NH; ++h) {
+                const uint64_t xd = umma::sw128_desc(x0 + h * C::NMMA * 128 + kk * 32);
+                umma::mma_bf16(tmem + h * C::NMMA, ad, xd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+              }
+            }
+            umma::mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+            if (++s == C::STAGES) { s = 0; ph ^= 1; }
+          }
+          umma::mma_commit(accfull);
+        }
+        __syncwarp();
+      }
+      // epilogue
+      bool ok = umma::mbar_wait(accfull, it & 1, limit_ns, sabort);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) {
+        if (lane == 0) *sabort = 1;
+        break;
+      }
+      umma::tc_fence_after();
+      const int row = q * 32 + lane;
+      epi.row(tmem + ((uint32_t)(q * 32) << 16), row, tile * TG_BM);
+      umma::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) umma::mbar_arrive(accempty);
+    }
+  }
+  __syncthreads();
+  if (*sabort && threadIdx.x == 0 && err) atomicCAS(err, 0, -4);
+  if (warp == 2) {
+    umma::tc_fence_after();
+    umma::tmem_dealloc(tmem, C::TMEM_COLS);
+  }
+}
+
+// host: 2-D tensor map of a K-major BF16 matrix [rows][k] (row stride k elements) with a
+// (64 x box_rows) box and the 128-byte swizzle.  cuTensorMapEncodeTiled is fetched from
+// the driver at run time, so the library does not link libcuda.
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+inline int make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t k, uint64_t rows, uint32_t box_rows) {
+  static PFN_encodeTiled fn = nullptr;
+  if (!fn) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &f, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !f)
+      return -1;
+    fn = (PFN_encodeTiled)f;
+  }
+  cuuint64_t dims[2] = {k, rows};
+  cuuint64_t strides[1] = {k * 2};
+  cuuint32_t box[2] = {(cuuint32_t)TG_BK, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : -2;
+}
+
+}  // namespace kura

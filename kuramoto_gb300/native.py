@@ -15,6 +15,9 @@ BUILD = os.path.join(PKG, "_build")
 
 COUPLING_DENSE = 0
 COUPLING_VOLCANO = 1
+ENGINE_AUTO = 0
+ENGINE_PERSISTENT = 1
+ENGINE_TENSOR = 2
 
 ERRORS = {
     -1: "KURA_ERR_INVALID", -2: "KURA_ERR_CUDA", -3: "KURA_ERR_NOMEM", -4: "KURA_ERR_BARRIER_TIMEOUT",
@@ -33,7 +36,7 @@ class Config(ctypes.Structure):
         ("n", ctypes.c_int64), ("k", ctypes.c_int32), ("coupling", ctypes.c_int32), ("batch", ctypes.c_int32),
         ("seed", ctypes.c_int32), ("atol", ctypes.c_double), ("rtol", ctypes.c_double),
         ("fixed_step", ctypes.c_int32), ("device", ctypes.c_int32), ("dense_level", ctypes.c_int32),
-        ("reserved0", ctypes.c_int32), ("stream", ctypes.c_void_p),
+        ("engine", ctypes.c_int32), ("stream", ctypes.c_void_p),
     ]
 
 
@@ -137,9 +140,9 @@ def volcano_factor(seed, n, k):
 
 class Network:
     def __init__(self, n, k=6, coupling=COUPLING_DENSE, batch=1, seed=1, atol=1e-6, rtol=0.0, fixed_step=False,
-                 device=0, dense_level=0, stream=None):
+                 device=0, dense_level=0, stream=None, engine=0):
         c = Config()
-        c.n, c.k, c.coupling, c.batch, c.seed = n, k, coupling, batch, seed
+        c.n, c.k, c.coupling, c.batch, c.seed, c.engine = n, k, coupling, batch, seed, engine
         c.atol, c.rtol, c.fixed_step, c.device, c.dense_level = atol, rtol, int(fixed_step), device, dense_level
         c.stream = stream
         self.cfg = c
@@ -151,9 +154,9 @@ class Network:
         self.h = h
 
     @staticmethod
-    def memory_required(n, k=6, coupling=COUPLING_DENSE, batch=1, dense_level=0):
+    def memory_required(n, k=6, coupling=COUPLING_DENSE, batch=1, dense_level=0, engine=0):
         c = Config()
-        c.n, c.k, c.coupling, c.batch, c.atol, c.dense_level = n, k, coupling, batch, 1e-6, dense_level
+        c.n, c.k, c.coupling, c.batch, c.atol, c.dense_level, c.engine = n, k, coupling, batch, 1e-6, dense_level, engine
         b = ctypes.c_int64()
         _check(lib().kura_memory_required(ctypes.byref(c), ctypes.byref(b)))
         return b.value
