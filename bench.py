@@ -51,6 +51,9 @@ WORKLOADS = {
     # 128 trajectories with distinct theta0 uniform in [0, 2pi), shared Cauchy omega, c=3
     "ensemble65536": dict(n=65536, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
                           dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False, engine="tensor"),
+    # the same ensemble at N=16384 (a 512 MiB BF16 adjacency, still larger than L2): profiling captures
+    "ensemble16384": dict(n=16384, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
+                          dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False, engine="tensor"),
     "dense16384": dict(n=16384, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
                        atol=1e-6, rtol=0.0, shared_theta=False),
     "dense16384x8": dict(n=16384, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.004,

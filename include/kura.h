@@ -154,6 +154,54 @@ int kura_integrate_volcano_noalloc(int64_t n, int32_t k, int32_t batch, int32_t 
                                    double atol, double rtol, int32_t device, void* stream, float* order_dev,
                                    int64_t order_cap, int64_t* accepted);
 
+/* ---- many independent networks of uneven size in one persistent launch
+ *
+ * The reference integrates one network per `kuramoto -A` process (kuramoto.cu:380-640,
+ * regenerated volcano coupling kuramoto.cu:62-135, integrator dp45.cu:148-164).  A
+ * kura_multi handle holds a set of such networks, each with its own N, rank K, Philox seed
+ * and coupling constant, all integrated from t = 0 to the same t1 with the same atol/rtol
+ * and output interval dt, each with its own adaptive step, by one launch in which a
+ * thread-block cluster integrates one network at a time from a work queue. */
+typedef struct kura_instance {
+  int64_t n;    /* oscillators, 1 .. 16 x 22755 */
+  int32_t k;    /* volcano rank 0..8 (-K) */
+  int32_t seed; /* Philox seed of the factor (-s) */
+  float c;      /* coupling constant (-c) */
+  int32_t reserved;
+} kura_instance;
+
+typedef struct kura_multi_stats {
+  double kernel_ms;     /* device time of the last integration launch */
+  double osc_steps;     /* sum over networks of accepted steps x n */
+  double tune_ms;       /* device time of the autotuner's chosen trial */
+  int64_t accepted;     /* accepted steps, all networks */
+  int64_t rejected;     /* rejected attempts, all networks */
+  int32_t cluster_size; /* CTAs per network */
+  int32_t block_threads;
+  int32_t grid; /* CTAs launched */
+  int32_t reserved;
+} kura_multi_stats;
+
+typedef struct kura_multi kura_multi;
+
+/* Allocates the device state of `count` networks (about 72 bytes per oscillator plus
+ * 4 bytes per record).  Records: r at t = 0 and at dt*m, m = 1 .. int(t1/dt) in float,
+ * as the reference's order.dat (kuramoto.cu:543-626).  h0 is the first trial step of every
+ * network.  cluster_size (1, 2, 4, 8, 16) and block_threads (256, 512, 1024) fix the launch
+ * shape; 0 lets the autotuner choose it at the first integration. */
+int kura_multi_create(const kura_instance* inst, int32_t count, double t1, double dt, double h0, double atol,
+                      double rtol, int32_t device, int32_t cluster_size, int32_t block_threads, kura_multi** out);
+void kura_multi_destroy(kura_multi* m);
+/* Integrates every network from the given start.  omega and theta0 hold the networks'
+ * oscillators back to back in the order of creation (host pointers, sum of n floats each).
+ * order receives count x (int(t1/dt) + 1) floats, network by network; theta_final (may be
+ * NULL) the unwrapped phases at each network's final time (the first step end >= t1);
+ * accepted (may be NULL) the accepted steps per network.  Synchronous.  A network whose
+ * step underflows or whose error norm is NaN fails the call with that code. */
+int kura_multi_integrate(kura_multi* m, const float* omega, const float* theta0, float* order, float* theta_final,
+                         int64_t* accepted);
+int kura_multi_get_stats(const kura_multi* m, kura_multi_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

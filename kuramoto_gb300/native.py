@@ -48,6 +48,19 @@ class Stats(ctypes.Structure):
     ]
 
 
+class Instance(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("k", ctypes.c_int32), ("seed", ctypes.c_int32), ("c", ctypes.c_float),
+                ("reserved", ctypes.c_int32)]
+
+
+class MultiStats(ctypes.Structure):
+    _fields_ = [
+        ("kernel_ms", ctypes.c_double), ("osc_steps", ctypes.c_double), ("tune_ms", ctypes.c_double),
+        ("accepted", ctypes.c_int64), ("rejected", ctypes.c_int64), ("cluster_size", ctypes.c_int32),
+        ("block_threads", ctypes.c_int32), ("grid", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    ]
+
+
 STEP_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                            ctypes.c_int64)
 OUTPUT_CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
@@ -104,6 +117,11 @@ def lib():
         "kura_get_stats": (i32, [P, ctypes.POINTER(Stats)]),
         "kura_random_inputs": (i32, [i32, i64, ctypes.c_float, ctypes.c_float, i32, i32, i32, fp, fp]),
         "kura_volcano_factor": (i32, [i32, i64, i32, ctypes.c_void_p]),
+        "kura_multi_create": (i32, [ctypes.POINTER(Instance), i32, f64, f64, f64, f64, f64, i32, i32, i32,
+                                    ctypes.POINTER(P)]),
+        "kura_multi_destroy": (None, [P]),
+        "kura_multi_integrate": (i32, [P, fp, fp, fp, fp, ctypes.POINTER(i64)]),
+        "kura_multi_get_stats": (i32, [P, ctypes.POINTER(MultiStats)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -265,3 +283,76 @@ class Network:
         s = Stats()
         _check(lib().kura_get_stats(self.h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+
+class MultiNetworks:
+    """Independent regenerated-volcano networks of uneven size integrated together, each
+    with its own adaptive step, by one persistent launch (kura_multi_* in kura.h).
+
+    ``ns``, ``ks``, ``seeds`` and ``cs`` give each network's size, volcano rank (0..8),
+    Philox seed and coupling constant; all share t1, dt, h0 (default dt/100, the
+    reference's first step), atol and rtol.  ``cluster_size`` / ``block_threads`` fix the
+    launch shape (0: autotuned at the first integration)."""
+
+    def __init__(self, ns, ks, seeds, cs, t1, dt, h0=None, atol=1e-6, rtol=0.0, device=0, cluster_size=0,
+                 block_threads=0):
+        count = len(ns)
+        if not (len(ks) == len(seeds) == len(cs) == count):
+            raise ValueError("ns, ks, seeds and cs must have the same length")
+        arr = (Instance * count)()
+        for i in range(count):
+            arr[i].n, arr[i].k, arr[i].seed, arr[i].c = int(ns[i]), int(ks[i]), int(seeds[i]), float(cs[i])
+        self.ns = np.asarray(ns, np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.ns)])
+        self.count = count
+        self.records = int(np.float32(t1) / np.float32(dt)) + 1
+        h = ctypes.c_void_p()
+        _check(lib().kura_multi_create(arr, count, float(t1), float(dt), float(dt / 100 if h0 is None else h0),
+                                       float(atol), float(rtol), device, cluster_size, block_threads,
+                                       ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().kura_multi_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def integrate(self, omega, theta0, want_theta=True):
+        """omega, theta0: the networks' oscillators back to back (or lists of per-network
+        arrays).  Returns (order [count, records], final phases per network or None,
+        accepted steps per network)."""
+        if isinstance(omega, (list, tuple)):
+            omega = np.concatenate(omega)
+        if isinstance(theta0, (list, tuple)):
+            theta0 = np.concatenate(theta0)
+        om = np.ascontiguousarray(omega, np.float32)
+        th = np.ascontiguousarray(theta0, np.float32)
+        if om.size != self.offsets[-1] or th.size != self.offsets[-1]:
+            raise ValueError("omega and theta0 need %d values" % self.offsets[-1])
+        order = np.zeros((self.count, self.records), np.float32)
+        fin = np.zeros(th.size, np.float32) if want_theta else None
+        acc = np.zeros(self.count, np.int64)
+        _check(lib().kura_multi_integrate(self.h, _fptr(om), _fptr(th), _fptr(order),
+                                          _fptr(fin) if want_theta else None,
+                                          acc.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        thetas = None
+        if want_theta:
+            thetas = [fin[self.offsets[i]:self.offsets[i + 1]] for i in range(self.count)]
+        return order, thetas, acc
+
+    def stats(self):
+        s = MultiStats()
+        _check(lib().kura_multi_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in MultiStats._fields_}

@@ -63,6 +63,15 @@ def test_invalid_config_rejected_without_gpu(native):
         native.Network(100, k=40, coupling=native.COUPLING_VOLCANO)
     with pytest.raises(native.KuraError):
         native.Network(100, batch=9)
+    # multi-network handles: rank above 8, a cluster size that is not a power of two, a
+    # block size outside 256/512/1024 and an empty set fail before any device work
+    for kw, code in ((dict(ks=[9]), -7), (dict(cluster_size=3), -1), (dict(block_threads=128), -1),
+                     (dict(ns=[0]), -7), (dict(ns=[], ks=[], seeds=[], cs=[]), -1)):
+        args = dict(ns=[100], ks=[5], seeds=[1], cs=[1.0])
+        args.update(kw)
+        with pytest.raises(native.KuraError) as e:
+            native.MultiNetworks(args.pop("ns"), args.pop("ks"), args.pop("seeds"), args.pop("cs"), 1.0, 1.0, **args)
+        assert e.value.code == code
 
 
 def test_cli_help_runs_without_gpu(native):
