@@ -54,6 +54,11 @@ WORKLOADS = {
     # the same ensemble at N=16384 (a 512 MiB BF16 adjacency, still larger than L2): profiling captures
     "ensemble16384": dict(n=16384, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
                           dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False, engine="tensor"),
+    # 512 independent regenerated-volcano networks of uneven size in one launch: N log-uniform
+    # in [1000, 20000], K uniform in 2..8, c uniform in [0, 6], Cauchy omega (scale 1), theta0
+    # uniform in [0, 2pi), each with its own adaptive step, t=100, records every dt=1
+    "multi512": dict(kind="multi", count=512, nmin=1000, nmax=20000, kmin=2, kmax=8, cmax=6.0, t1=100.0, dt=1.0,
+                     atol=1e-6, rtol=0.0),
     "dense16384": dict(n=16384, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
                        atol=1e-6, rtol=0.0, shared_theta=False),
     "dense16384x8": dict(n=16384, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.004,
@@ -289,6 +294,179 @@ def roofline(w, res, args):
             "bytes_per_unit": per_unit, "kernel_ms_per_launch": round(kernel_s * 1e3, 3)}
 
 
+def multi_inputs(w, seed):
+    """Seeded networks of the multi-network workload (sizes, ranks, couplings, Philox seeds)
+    and their inputs, one array per network."""
+    rng = np.random.default_rng(seed)
+    count = w["count"]
+    ns = np.exp(rng.uniform(np.log(w["nmin"]), np.log(w["nmax"]), count)).astype(np.int64)
+    ks = rng.integers(w["kmin"], w["kmax"] + 1, count)
+    cs = rng.uniform(0.0, w["cmax"], count).astype(np.float32)
+    seeds = rng.integers(1, 1 << 30, count)
+    ths = [(rng.random(int(n)) * 2 * np.pi).astype(np.float32) for n in ns]
+    oms = [np.tan(np.pi * (rng.random(int(n)) - 0.5)).astype(np.float32) for n in ns]
+    return ns, ks, seeds, cs, ths, oms
+
+
+def run_multi(args, w):
+    import torch
+    import kuramoto_gb300 as kg
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    nets = multi_inputs(w, instance_seed(rank))
+    ns, ks, seeds, cs, ths, oms = nets
+    om = np.concatenate(oms)
+    th = np.concatenate(ths)
+    m = kg.MultiNetworks(ns, ks, seeds, cs, w["t1"], w["dt"], atol=w["atol"], rtol=w["rtol"], device=local)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):  # the first one runs the autotuner and captures the graph
+        order, _, acc = m.integrate(om, th, want_theta=False)
+    barrier()
+    # one timed step = one integration of every network.  `value` counts the device time of
+    # the persistent launch (CUDA events on the library's stream around the graph launch,
+    # inputs already in HBM); e2e times the whole synchronous call with host buffers (H2D
+    # of omega and theta0, the launch, D2H of the records and the final phases)
+    kern_ms = e2e_ms = osc = 0.0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            barrier()
+            t0 = time.perf_counter()
+            order, thetas, acc = m.integrate(om, th, want_theta=True)
+            e2e_ms += (time.perf_counter() - t0) * 1e3
+            st = m.stats()
+            kern_ms += st["kernel_ms"]
+            osc += st["osc_steps"]
+    units, ms = combine_ranks(osc, kern_ms, "cuda")
+    e2e_units, e2e_ms = combine_ranks(osc, e2e_ms, "cuda")
+    tot = int(ns.sum())
+    res = dict(value=units / (ms / 1e3), ms=ms, kernel_ms=kern_ms, launches=args.steps,
+               e2e_value=e2e_units / (e2e_ms / 1e3), h2d=8 * tot, d2h=4 * order.size + 4 * tot + 8 * len(ns),
+               clocks=clk.summary(), orders=order, nets=nets, osc_per_step=osc / args.steps,
+               shape=(st["cluster_size"], st["block_threads"], st["grid"]), tune_ms=st["tune_ms"], acc=acc)
+    m.close()
+    return res
+
+
+def _multi_worker(job):
+    """One network on one host core (the reference runs one process per network)."""
+    from oracle import kora
+    th, om, k, c, seed, t1, dt, atol, rtol = job
+    r = kora.run(th, om, k=int(k), c1=float(c), onthefly=True, seed=int(seed), fp64=False, t1=t1, dt=dt, atol=atol,
+                 rtol=rtol, threads=1)
+    return r.steps * th.size
+
+
+def multi_cpu(w, nets, threads, t1):
+    """Every network of the workload to t1 on `threads` host processes, one network per task
+    (spawned, so that no child inherits a CUDA context)."""
+    import multiprocessing as mp
+    ns, ks, seeds, cs, ths, oms = nets
+    jobs = [(ths[i], oms[i], ks[i], cs[i], seeds[i], t1, w["dt"], w["atol"], w["rtol"]) for i in np.argsort(-ns)]
+    with mp.get_context("spawn").Pool(threads) as pool:
+        pool.map(_multi_worker, jobs[:threads], chunksize=1)  # children up and the oracle loaded
+        t0 = time.perf_counter()
+        osc = sum(pool.map(_multi_worker, jobs, chunksize=1))
+        el = time.perf_counter() - t0
+    return osc / el, el, osc
+
+
+MULTI_CPU_T1 = 1.0  # horizon of the CPU sample of the multi-network workload (every network)
+
+
+def main_multi(args, w):
+    ws, rank, local = dist_env()
+    config = {"workload": args.workload, "networks": w["count"],
+              "n": "log-uniform [%d, %d]" % (w["nmin"], w["nmax"]), "k": "uniform %d..%d" % (w["kmin"], w["kmax"]),
+              "coupling": "volcano-regenerated", "c": "uniform [0, %g]" % w["cmax"],
+              "frequencies": "cauchy (scale 1)", "theta0": "uniform [0, 2pi)", "t1": w["t1"], "dt": w["dt"],
+              "atol": w["atol"], "rtol": w["rtol"],
+              "l2": "flushed between steps (512 MiB write); the networks' state (~225 MB) exceeds L2",
+              "parallelism": "replicas" if ws > 1 else "single"}
+    metric = "accepted DP45 steps x N x batch / s"
+    threads = os.cpu_count() or 1
+    sample = ("every one of the %d networks to t=%g (%g%% of the horizon), one network per task on %d host "
+              "processes (the reference runs one process per network), float32 oracle restating the reference "
+              "program" % (w["count"], MULTI_CPU_T1, 100 * MULTI_CPU_T1 / w["t1"], threads))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        nets = multi_inputs(w, 1)
+        for _ in range(args.warmup):
+            multi_cpu(w, nets, threads, MULTI_CPU_T1 / 4)
+        osc = el = 0.0
+        for _ in range(args.steps):
+            v, e, o = multi_cpu(w, nets, threads, MULTI_CPU_T1)
+            osc += o
+            el += e
+        value = osc / el
+        print(json.dumps({"impl": "reference", "metric": metric, "value": value, "unit": "osc-steps/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                          "cpu_baseline": {"value": value, "unit": "osc-steps/s", "cores": threads, "kind": "port",
+                                           "sample": sample},
+                          "e2e": {"value": value, "unit": "osc-steps/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    res = run_multi(args, w)
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved = STATE_BYTES * res["osc_per_step"] / (res["kernel_ms"] / args.steps / 1e3) / 1e9
+    traffic = None
+    try:
+        t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(args.workload)
+        if t:
+            traffic = t["bytes_per_accepted_osc_step"] * res["osc_per_step"]
+    except Exception:
+        pass
+    line = {"metric": metric, "value": res["value"], "unit": "osc-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config}
+    line["e2e"] = {"value": res["e2e_value"], "unit": "osc-steps/s", "h2d_bytes_per_step": res["h2d"],
+                   "d2h_bytes_per_step": res["d2h"]}
+    line["gpu_launches"] = res["launches"]
+    line["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                        "frac": round(achieved / hbm, 4), "traffic": traffic,
+                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                        "bytes_per_unit": STATE_BYTES,
+                        "kernel_ms_per_launch": round(res["kernel_ms"] / args.steps, 3)}
+    line["clocks"] = res["clocks"]
+    line["launch_shape"] = {"cluster_size": res["shape"][0], "block_threads": res["shape"][1],
+                            "grid": res["shape"][2], "autotune_trial_ms": round(res["tune_ms"], 3)}
+    line["accepted_steps_per_network"] = {"mean": float(res["acc"].mean()), "max": int(res["acc"].max())}
+    if not args.no_cpu:
+        v, el, osc = multi_cpu(w, res["nets"], threads, MULTI_CPU_T1)
+        line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
+                                "sample": sample + " (%.1f s)" % el}
+        # r error of the two smallest networks against the FP64 oracle over the records t <= 10
+        from oracle import kora
+        ns, ks, seeds, cs, ths, oms = res["nets"]
+        errs = []
+        for i in np.argsort(ns)[:2]:
+            r = kora.run(ths[i], oms[i], k=int(ks[i]), c1=float(cs[i]), onthefly=True, seed=int(seeds[i]),
+                         fp64=True, t1=10.0, dt=w["dt"], atol=w["atol"], rtol=w["rtol"], threads=threads)
+            errs.append(float(np.max(np.abs(r.order - res["orders"][i][:r.order.size]))))
+        line["r_err_vs_fp64"] = max(errs)
+    print(json.dumps(line))
+
+
 def cpu_baseline(w, om, thetas, threads, sample_steps=None):
     from oracle import kora
     n = w["n"]
@@ -324,6 +502,8 @@ def main():
     w = dict(WORKLOADS[args.workload])
     if args.t1 is not None:
         w["t1"] = args.t1
+    if w.get("kind") == "multi":
+        return main_multi(args, w)
     ws, rank, local = dist_env()
     n, B = w["n"], len(w["cs"])
     config = {"workload": args.workload, "n": n, "k": w["k"], "coupling": "volcano-regenerated" if w["coupling"] else
