@@ -202,6 +202,35 @@ int kura_multi_integrate(kura_multi* m, const float* omega, const float* theta0,
                          int64_t* accepted);
 int kura_multi_get_stats(const kura_multi* m, kura_multi_stats* stats);
 
+/* ---- the order-parameter surrogate (a learned model; the reference has no counterpart)
+ *
+ * A 4-layer perceptron in_dim -> hidden -> hidden -> hidden -> out_dim with SiLU between
+ * layers, BF16 weights and activations, FP32 accumulation, FP32 master weights and biases.
+ * Its forward and backward GEMMs run on the tensor cores; training is Adam with a linear
+ * learning-rate ramp, on minibatches of `batch` rows, one CUDA graph per step.  Loss: mean
+ * squared error over the out_dim outputs. */
+typedef struct kura_mlp kura_mlp;
+
+/* in_dim, out_dim 1..64; hidden 64, 128 or 256; batch a multiple of 128 up to 4096.  Weights
+ * are Glorot-uniform from a splitmix64 stream of `seed`, biases zero. */
+int kura_mlp_create(int32_t in_dim, int32_t hidden, int32_t out_dim, int32_t batch, uint64_t seed, int32_t device,
+                    kura_mlp** out);
+void kura_mlp_destroy(kura_mlp* m);
+/* Parameters in this order, layer by layer: W [out][in] row-major, then b [out]. */
+int kura_mlp_param_count(const kura_mlp* m, int64_t* count);
+int kura_mlp_get_params(kura_mlp* m, float* params, int64_t count);
+int kura_mlp_set_params(kura_mlp* m, const float* params, int64_t count);
+/* y[n][out_dim] = f(x[n][in_dim]), host arrays, any n. */
+int kura_mlp_forward(kura_mlp* m, const float* x, int64_t n, float* y);
+/* Loss and its gradient (parameter order above) on one minibatch of n <= batch rows. */
+int kura_mlp_gradients(kura_mlp* m, const float* x, const float* target, int64_t n, float* grads, float* loss);
+/* Trains on n_samples rows (at least one batch): `epochs` passes, each a fresh shuffle from
+ * `shuffle_seed` that drops the last partial batch; Adam (0.9, 0.999, 1e-8) restarted at the
+ * call, learning rate from lr to lr_final.  epoch_loss[epochs] (may be NULL) receives the mean
+ * minibatch loss of each epoch, device_ms (may be NULL) the device time of the steps. */
+int kura_mlp_train(kura_mlp* m, const float* x, const float* target, int64_t n_samples, int32_t epochs, float lr,
+                   float lr_final, uint64_t shuffle_seed, float* epoch_loss, double* device_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,7 @@ compute call needs the native library and a GPU and raises otherwise.
 """
 from .native import (  # noqa: F401
     KuraError,
+    MLP,
     MultiNetworks,
     Network,
     lib,
@@ -21,5 +22,5 @@ from .native import (  # noqa: F401
     ENGINE_TENSOR,
 )
 
-__all__ = ["KuraError", "MultiNetworks", "Network", "lib", "lib_path", "cli_path", "random_inputs", "volcano_factor",
+__all__ = ["KuraError", "MLP", "MultiNetworks", "Network", "lib", "lib_path", "cli_path", "random_inputs", "volcano_factor",
            "COUPLING_DENSE", "COUPLING_VOLCANO", "ENGINE_AUTO", "ENGINE_PERSISTENT", "ENGINE_TENSOR"]

@@ -51,6 +51,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         "kura_noalloc.o": [nv, *cu_flags, "-c", os.path.join(SRC, "kura_noalloc.cu")],
         "kura_tensor.o": [nv, *cu_flags, "-c", os.path.join(SRC, "kura_tensor.cu")],
         "kura_multi.o": [nv, *cu_flags, "-c", os.path.join(SRC, "kura_multi.cu")],
+        "kura_mlp.o": [nv, *cu_flags, "-c", os.path.join(SRC, "kura_mlp.cu")],
         "kura_host_rng.o": ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INC, "-c",
                             os.path.join(SRC, "kura_host_rng.cpp")],
     }

@@ -122,6 +122,15 @@ def lib():
         "kura_multi_destroy": (None, [P]),
         "kura_multi_integrate": (i32, [P, fp, fp, fp, fp, ctypes.POINTER(i64)]),
         "kura_multi_get_stats": (i32, [P, ctypes.POINTER(MultiStats)]),
+        "kura_mlp_create": (i32, [i32, i32, i32, i32, ctypes.c_uint64, i32, ctypes.POINTER(P)]),
+        "kura_mlp_destroy": (None, [P]),
+        "kura_mlp_param_count": (i32, [P, ctypes.POINTER(i64)]),
+        "kura_mlp_get_params": (i32, [P, fp, i64]),
+        "kura_mlp_set_params": (i32, [P, fp, i64]),
+        "kura_mlp_forward": (i32, [P, fp, i64, fp]),
+        "kura_mlp_gradients": (i32, [P, fp, fp, i64, fp, fp]),
+        "kura_mlp_train": (i32, [P, fp, fp, i64, i32, ctypes.c_float, ctypes.c_float, ctypes.c_uint64, fp,
+                                 ctypes.POINTER(f64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -356,3 +365,68 @@ class MultiNetworks:
         s = MultiStats()
         _check(lib().kura_multi_get_stats(self.h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in MultiStats._fields_}
+
+
+class MLP:
+    """The order-parameter surrogate network (kura_mlp_* in kura.h): in_dim -> hidden ->
+    hidden -> hidden -> out_dim with SiLU, BF16 weights and FP32 accumulation, trained and
+    evaluated by libkura's tensor-core kernels."""
+
+    def __init__(self, in_dim, out_dim, hidden=256, batch=512, seed=1, device=0):
+        self.in_dim, self.out_dim, self.hidden, self.batch = in_dim, out_dim, hidden, batch
+        h = ctypes.c_void_p()
+        _check(lib().kura_mlp_create(in_dim, hidden, out_dim, batch, seed, device, ctypes.byref(h)))
+        self.h = h
+        c = ctypes.c_int64()
+        _check(lib().kura_mlp_param_count(self.h, ctypes.byref(c)))
+        self.param_count = c.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().kura_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def params(self):
+        p = np.zeros(self.param_count, np.float32)
+        _check(lib().kura_mlp_get_params(self.h, _fptr(p), p.size))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        _check(lib().kura_mlp_set_params(self.h, _fptr(p), p.size))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.in_dim)
+        y = np.zeros((x.shape[0], self.out_dim), np.float32)
+        _check(lib().kura_mlp_forward(self.h, _fptr(x), x.shape[0], _fptr(y)))
+        return y
+
+    def gradients(self, x, t):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.in_dim)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, self.out_dim)
+        g = np.zeros(self.param_count, np.float32)
+        loss = ctypes.c_float()
+        _check(lib().kura_mlp_gradients(self.h, _fptr(x), _fptr(t), x.shape[0], _fptr(g), ctypes.byref(loss)))
+        return loss.value, g
+
+    def train(self, x, t, epochs, lr=1e-3, lr_final=None, seed=1):
+        """Adam on minibatches of `batch` rows; returns (loss per epoch, device ms)."""
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, self.in_dim)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, self.out_dim)
+        losses = np.zeros(epochs, np.float32)
+        ms = ctypes.c_double()
+        _check(lib().kura_mlp_train(self.h, _fptr(x), _fptr(t), x.shape[0], epochs, lr,
+                                    lr if lr_final is None else lr_final, seed, _fptr(losses), ctypes.byref(ms)))
+        return losses, ms.value
