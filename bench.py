@@ -59,6 +59,12 @@ WORKLOADS = {
     # uniform in [0, 2pi), each with its own adaptive step, t=100, records every dt=1
     "multi512": dict(kind="multi", count=512, nmin=1000, nmax=20000, kmin=2, kmax=8, cmax=6.0, t1=100.0, dt=1.0,
                      atol=1e-6, rtol=0.0),
+    # the learned sweep placement: 20000 training networks at N=10000 from the batched solver
+    # (c uniform in [0, 6], K uniform in 2..8, frequency scale log-uniform in [0.5, 2], 10 %
+    # Cauchy), a 4 x 256 MLP trained on them, then surrogate-guided sweeps of 64 points,
+    # each verified by a DP45 run to t=60
+    "surrogate": dict(kind="surrogate", networks=20000, n=10000, t1=60.0, cauchy_frac=0.1, epochs=60,
+                      sweeps=[(5, 1.0, 0), (3, 0.7, 0), (8, 1.5, 0), (6, 1.5, 1)]),
     "dense16384": dict(n=16384, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
                        atol=1e-6, rtol=0.0, shared_theta=False),
     "dense16384x8": dict(n=16384, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.004,
@@ -467,6 +473,74 @@ def main_multi(args, w):
     print(json.dumps(line))
 
 
+def main_surrogate(args, w):
+    """The learned part end to end on one GPU.  ``value`` is the batched solver's throughput
+    while it generates the training data (the dominant cost); the other keys report the
+    training, the held-out accuracy and, for each swept network, the DP45 verification and
+    the gain over an even sweep."""
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned component or batched "
+                              "solver; its per-network CPU cost is the multi512 workload's reference arm"}))
+        return
+    import torch
+    from kuramoto_gb300 import surrogate as S
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(instance_seed(rank))
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        X, Y, st = S.generate(w["networks"], w["n"], w["t1"], rng, device=local, cauchy_frac=w["cauchy_frac"])
+        gen_wall = time.perf_counter() - t0
+        nval = len(X) // 10
+        sur = S.Surrogate(hidden=256, batch=512, seed=instance_seed(rank), device=local)
+        losses, train_ms = sur.fit(X[nval:], Y[nval:], epochs=w["epochs"], lr=2e-3, lr_final=1e-4)
+        pred = sur.predict(X[:nval])
+        sweeps = []
+        for (k, f, cauchy) in w["sweeps"]:
+            seed = 1000 + len(sweeps)
+            res = S.sweep(sur, w["n"], k, f, cauchy, seed, rng, npoints=64, candidates=64, t1=w["t1"], device=local)
+            c = np.linspace(0, 6, 121).astype(np.float32)
+            ones = np.ones(c.size)
+            orders, st_dense = S.simulate(w["n"], c, (k * ones).astype(int), (seed * ones).astype(int),
+                                          [res["theta0"]] * c.size, [res["omega"]] * c.size, w["t1"], device=local)
+            lo, hi = S.transition_window(c, S.targets(orders, w["t1"])[:, 1])
+            width = max(hi - lo, 0.05)
+            inside = int(np.sum((res["points"] >= lo) & (res["points"] <= hi)))
+            spent = res["osc_steps_full"] + res["osc_steps_short"]
+            even_runs = 6.0 / (width / max(inside, 1))
+            sweeps.append({"k": k, "f": f, "family": "cauchy" if cauchy else "normal",
+                           "transition_window": [round(lo, 3), round(hi, 3)],
+                           "points_in_window": inside, "even_points_in_window": round(64 * width / 6.0, 1),
+                           "within_0.02": float(res["within_tol"].mean()),
+                           "max_err_mean_r": float(res["err"][:, 0].max()),
+                           "cost_vs_even_sweep_same_spacing": round(even_runs * res["osc_steps_full"] / 64 / spent, 2)})
+        sur.close()
+    steps_total = (len(X) - nval) // 512 * w["epochs"]
+    mlp_flops = 6.0 * 512 * (64 * 256 + 2 * 256 * 256 + 256 * 64) * steps_total  # fwd + 2 bwd GEMMs per layer
+    line = {"metric": "accepted DP45 steps x N x batch / s", "value": st["osc_steps"] / (st["kernel_ms"] / 1e3),
+            "unit": "osc-steps/s", "n_gpus": ws, "steps": 1, "warmup": 0, "ms_per_step": st["kernel_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 solver, bf16 MLP",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "networks": w["networks"], "n": w["n"], "t1": w["t1"],
+                       "c": "uniform [0, 6]", "k": "uniform 2..8", "freq_scale": "log-uniform [0.5, 2]",
+                       "cauchy_fraction": w["cauchy_frac"], "mlp": "14 -> 256 -> 256 -> 256 -> 2, SiLU",
+                       "epochs": w["epochs"], "batch": 512, "l2": "not flushed (one pass)"},
+            "e2e": {"value": st["osc_steps"] / gen_wall, "unit": "osc-steps/s", "h2d_bytes_per_step": 8 * len(X) * w["n"],
+                    "d2h_bytes_per_step": 4 * len(X) * (int(w["t1"]) + 1)},
+            "gpu_launches": 1 + steps_total * 19,
+            "training": {"samples": len(X) - nval, "steps": steps_total, "device_ms": round(train_ms, 1),
+                         "first_epoch_loss": float(losses[0]), "last_epoch_loss": float(losses[-1]),
+                         "achieved_tflops": round(mlp_flops / (train_ms / 1e3) / 1e12, 3)},
+            "holdout": {"networks": nval, "mean_r_within_0.02": float(np.mean(np.abs(pred[:, 0] - Y[:nval, 0]) <= 0.02)),
+                        "std_r_r2": float(1 - np.mean((pred[:, 1] - Y[:nval, 1]) ** 2) / np.var(Y[:nval, 1]))},
+            "sweeps": sweeps, "clocks": clk.summary(),
+            "accepted_steps_per_network": {"mean": float(st["accepted_per_network"].mean()),
+                                           "max": int(st["accepted_per_network"].max())}}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def cpu_baseline(w, om, thetas, threads, sample_steps=None):
     from oracle import kora
     n = w["n"]
@@ -504,6 +578,8 @@ def main():
         w["t1"] = args.t1
     if w.get("kind") == "multi":
         return main_multi(args, w)
+    if w.get("kind") == "surrogate":
+        return main_surrogate(args, w)
     ws, rank, local = dist_env()
     n, B = w["n"], len(w["cs"])
     config = {"workload": args.workload, "n": n, "k": w["k"], "coupling": "volcano-regenerated" if w["coupling"] else

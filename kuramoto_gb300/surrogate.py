@@ -133,7 +133,7 @@ def place_points(cgrid, density, npoints):
     return np.interp(q, cdf, cgrid).astype(np.float32)
 
 
-def sweep(sur, n, k, f, cauchy, seed, rng, npoints=64, candidates=128, c_range=(0.0, 6.0), t1=60.0, tol=0.02,
+def sweep(sur, n, k, f, cauchy, seed, rng, npoints=64, candidates=64, c_range=(0.0, 6.0), t1=60.0, tol=0.02,
           device=0):
     """Surrogate-guided sweep of c for one network (fixed seed, omega and theta0).
 
