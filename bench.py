@@ -47,6 +47,9 @@ WORKLOADS = {
                        atol=1e-6, rtol=0.0, shared_theta=False),
     "dense65536x8": dict(n=65536, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.004,
                          dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False),
+    # the same network with N*A stored as int8 (exact for the volcano rule): 4.3 GB per RHS
+    "dense65536i8": dict(n=65536, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
+                         atol=1e-6, rtol=0.0, shared_theta=False, adj_storage=1),
     # the shared-adjacency ensemble on tensor cores: N=65536, K=5 dense volcano adjacency,
     # 128 trajectories with distinct theta0 uniform in [0, 2pi), shared Cauchy omega, c=3
     "ensemble65536": dict(n=65536, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
@@ -67,6 +70,8 @@ WORKLOADS = {
                       sweeps=[(5, 1.0, 0), (3, 0.7, 0), (8, 1.5, 0), (6, 1.5, 1)]),
     "dense16384": dict(n=16384, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
                        atol=1e-6, rtol=0.0, shared_theta=False),
+    "dense16384i8": dict(n=16384, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
+                         atol=1e-6, rtol=0.0, shared_theta=False, adj_storage=1),
     "dense16384x8": dict(n=16384, k=5, coupling=0, cs=[3.0] * 8, normal=False, init=2 * np.pi, t1=0.004,
                          dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False),
 }
@@ -175,7 +180,7 @@ def run_native(args, w):
     n, B = w["n"], len(w["cs"])
     stream = torch.cuda.current_stream()
     net = kg.Network(n, k=w["k"], coupling=w["coupling"], batch=B, seed=seed, atol=w["atol"], rtol=w["rtol"],
-                     dense_level=0, device=local, stream=stream.cuda_stream)
+                     dense_level=0, device=local, stream=stream.cuda_stream, adj_storage=w.get("adj_storage", 0))
     net.set_frequencies(om)
     if w["coupling"] == 0:
         net.generate_adjacency()
@@ -284,7 +289,8 @@ def roofline(w, res, args):
         per_unit = STATE_BYTES
         bytes_per_launch = per_unit * acc_per_launch * n
     else:
-        per_unit = 24.0 * n / len(w["cs"])
+        # 6 RHS x N entries of A per accepted step and oscillator: 4 bytes each (float32) or 1 (int8)
+        per_unit = (6.0 if w.get("adj_storage") else 24.0) * n / len(w["cs"])
         bytes_per_launch = per_unit * acc_per_launch * n
     achieved = bytes_per_launch / kernel_s / 1e9
     traffic = None
@@ -586,6 +592,8 @@ def main():
               "dense", "batch": B, "c": w["cs"], "t1": w["t1"], "dt": w["dt"], "atol": w["atol"],
               "rtol": w["rtol"], "frequencies": "normal (glibc rand, seed 1)" if w["normal"] else "cauchy",
               "l2": "flushed between steps (512 MiB write)", "parallelism": "replicas" if ws > 1 else "single"}
+    if w.get("adj_storage"):
+        config["adjacency_storage"] = "int8 (N*A, exact for the volcano rule)"
     metric = "accepted DP45 steps x N x batch / s"
     threads = os.cpu_count() or 1
 

@@ -41,6 +41,13 @@ extern "C" {
  * or volcano coupling, every dense level); the tensor-core ensemble takes a dense network
  * with batch <= 128, keeps only the order parameter (dense level 0) and reports no per-step
  * records.  The reference has neither: it integrates one trajectory per process. */
+/* Storage of a dense adjacency on the persistent engine.  KURA_ADJ_I8 keeps N*A as int8,
+ * a quarter of the bytes the coupling streams per RHS; it holds the reference's volcano rule
+ * exactly (N*A_ij is an integer in [-K, K], K <= 127) and any adjacency whose entries are
+ * integer multiples of 1/N within that range.  The reference stores float32. */
+#define KURA_ADJ_F32 0
+#define KURA_ADJ_I8 1
+
 #define KURA_ENGINE_AUTO 0
 #define KURA_ENGINE_PERSISTENT 1
 #define KURA_ENGINE_TENSOR 2
@@ -61,6 +68,7 @@ typedef struct kura_config {
   int32_t dense_level; /* -D: 0 order only; >=1 adds phases and step times; >=2 adds couplings */
   int32_t engine;      /* KURA_ENGINE_*: which kernels integrate the batch */
   void* stream;        /* cudaStream_t for every launch and copy (NULL: a stream owned by the handle) */
+  int32_t adj_storage; /* KURA_ADJ_F32 (default) or KURA_ADJ_I8, dense coupling on the persistent engine */
 } kura_config;
 
 typedef struct kura_stats {
@@ -126,6 +134,11 @@ int kura_final_record(kura_handle* h, int32_t traj, float* theta, float* couplin
 /* right-hand side dtheta/dt and couplings [A cos, A sin] interleaved at theta (dydt, kuramoto.cu:118-126) */
 int kura_rhs(kura_handle* h, int32_t traj, const float* theta, float* dtheta, float* couplings);
 int kura_get_stats(kura_handle* h, kura_stats* st);
+/* checkpoint grain: at most `attempts` step attempts per persistent launch (<= 0: unbounded,
+ * the default), so that on_chunk sees the phases, t and h at least that often.  The
+ * reference rewrites fs.dat after every accepted step for preemption (kuramoto.cu:251-264);
+ * this is the same checkpoint at a coarser, chosen grain.  Persistent engine only. */
+int kura_set_launch_attempts(kura_handle* h, int64_t attempts);
 
 /* host random inputs with glibc rand(): theta0 uniform in [-init/2, init/2] then
  * Cauchy or normal frequencies (kuramoto.cu:416, 495-541) */

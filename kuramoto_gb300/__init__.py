@@ -20,7 +20,9 @@ from .native import (  # noqa: F401
     ENGINE_AUTO,
     ENGINE_PERSISTENT,
     ENGINE_TENSOR,
+    ADJ_F32,
+    ADJ_I8,
 )
 
 __all__ = ["KuraError", "MLP", "MultiNetworks", "Network", "lib", "lib_path", "cli_path", "random_inputs", "volcano_factor",
-           "COUPLING_DENSE", "COUPLING_VOLCANO", "ENGINE_AUTO", "ENGINE_PERSISTENT", "ENGINE_TENSOR"]
+           "COUPLING_DENSE", "COUPLING_VOLCANO", "ENGINE_AUTO", "ENGINE_PERSISTENT", "ENGINE_TENSOR", "ADJ_F32", "ADJ_I8"]

@@ -41,6 +41,8 @@ struct kura_handle {
   // device
   float* omega = nullptr;
   float* adj = nullptr;
+  int8_t* adj8 = nullptr;  // N*A as int8 (KURA_ADJ_I8), rows of ld8
+  int ld8 = 0;
   float* ph_hi = nullptr;
   float* ph_lo = nullptr;
   long long* ph_w = nullptr;
@@ -71,6 +73,7 @@ struct kura_handle {
   std::vector<float> t_eval_h;
   std::vector<double> t0;
   bool omega_set = false, adj_set = false, horizon_set = false;
+  long long launch_attempts = -1;  // step attempts per persistent launch (< 0: unbounded)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   kura_stats stats{};
   kura::TensorEngine* te = nullptr;  // the tensor-core ensemble, when selected
@@ -117,7 +120,14 @@ static int validate(const kura_config* c) {
     return fail(KURA_ERR_INVALID, "k*n too large");
   if (!(c->atol > 0) && !c->fixed_step) return fail(KURA_ERR_INVALID, "atol must be > 0");
   if (c->rtol < 0) return fail(KURA_ERR_INVALID, "rtol must be >= 0");
+  if (c->adj_storage != KURA_ADJ_F32 && c->adj_storage != KURA_ADJ_I8)
+    return fail(KURA_ERR_INVALID, "unknown adjacency storage");
+  if (c->adj_storage == KURA_ADJ_I8 && c->coupling == KURA_COUPLING_DENSE && c->k > 127)
+    return fail(KURA_ERR_UNSUPPORTED, "int8 adjacency storage holds N*A exactly only for k <= 127");
   return KURA_OK;
+}
+static bool uses_i8(const kura_config* c) {
+  return c->adj_storage == KURA_ADJ_I8 && c->coupling == KURA_COUPLING_DENSE && resolve_engine(c) != KURA_ENGINE_TENSOR;
 }
 
 extern "C" int kura_memory_required(const kura_config* c, int64_t* bytes) {
@@ -131,7 +141,7 @@ extern "C" int kura_memory_required(const kura_config* c, int64_t* bytes) {
   plan(c, &ld, &bmax, &kmax);
   long long B = c->batch, n = ld;
   long long b = 4 * n;                                   // omega
-  if (c->coupling == KURA_COUPLING_DENSE) b += 4LL * c->n * n;
+  if (c->coupling == KURA_COUPLING_DENSE) b += uses_i8(c) ? c->n * ((c->n + 15) / 16 * 16) : 4LL * c->n * n;
   b += 2 * B * n * (4 + 4 + 8);                          // phases
   b += 7 * B * n * 4;                                    // slopes
   b += 2 * B * n * 8;                                    // exchange
@@ -143,7 +153,7 @@ extern "C" int kura_memory_required(const kura_config* c, int64_t* bytes) {
 extern "C" void kura_destroy(kura_handle* h) {
   if (!h) return;
   cudaSetDevice(h->cfg.device);
-  void* ptrs[] = {h->omega, h->adj, h->ph_hi, h->ph_lo, h->ph_w, h->g, h->xbuf, h->part, h->bar, h->err,
+  void* ptrs[] = {h->omega, h->adj, h->adj8, h->ph_hi, h->ph_lo, h->ph_w, h->g, h->xbuf, h->part, h->bar, h->err,
                   h->traj, h->t_eval, h->out_r, h->out_idx, h->out_theta, h->out_coup, h->log_t, h->log_h,
                   h->fin_theta, h->fin_coup, h->counters};
   for (void* p : ptrs)
@@ -220,7 +230,7 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   int G = sms;
   int rows = ceil_div(h->n, G);
   int bps = 0;
-  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));
+  CUH(kura::persistent_config(uses_i8(cfg) ? kura::COUP_DENSE_I8 : h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));
   if (bps < 1) return bail(fail(KURA_ERR_UNSUPPORTED, "persistent kernel does not fit on an SM"));
   G = sms * std::min(bps, 1);
   // at least 64 rows per CTA for the regenerated coupling (its cost per CTA is mostly
@@ -228,14 +238,19 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   G = std::min(G, std::max(1, ceil_div(h->n, h->coupling == KURA_COUPLING_DENSE ? 16 : 64)));
   rows = ceil_div(h->n, G);
   G = ceil_div(h->n, rows);
-  CUH(kura::persistent_config(h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));
+  CUH(kura::persistent_config(uses_i8(cfg) ? kura::COUP_DENSE_I8 : h->coupling, h->bmax, h->kmax, &h->smem, &bps, rows, &h->xs_smem));
   if (bps < 1) return bail(fail(KURA_ERR_UNSUPPORTED, "persistent kernel shared memory exceeds an SM"));
   h->grid = G;
   h->rows = rows;
 
   size_t ld = h->ld, B = h->B;
   CUH(dalloc(&h->omega, ld));
-  if (h->coupling == KURA_COUPLING_DENSE) CUH(dalloc(&h->adj, (size_t)h->n * ld));
+  if (uses_i8(cfg)) {
+    h->ld8 = (h->n + 15) / 16 * 16;
+    CUH(dalloc(&h->adj8, (size_t)h->n * h->ld8));
+  } else if (h->coupling == KURA_COUPLING_DENSE) {
+    CUH(dalloc(&h->adj, (size_t)h->n * ld));
+  }
   CUH(dalloc(&h->ph_hi, 2 * B * ld));
   CUH(dalloc(&h->ph_lo, 2 * B * ld));
   CUH(dalloc(&h->ph_w, 2 * B * ld));
@@ -299,8 +314,25 @@ extern "C" int kura_set_adjacency(kura_handle* h, const float* adj, int64_t n) {
     h->adj_set = true;
     return KURA_OK;
   }
-  CU(cudaMemcpy2DAsync(h->adj, sizeof(float) * h->ld, adj, sizeof(float) * n, sizeof(float) * n, n,
-                       cudaMemcpyHostToDevice, h->stream));
+  if (h->adj8) {
+    // integers N*A_ij in [-127, 127] that reproduce A_ij exactly as float(k) * float(1/N)
+    const float invn = 1.0f / (float)n;
+    std::vector<int8_t> q((size_t)n * h->ld8, 0);
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t j = 0; j < n; ++j) {
+        const float a = adj[i * n + j];
+        const double k = std::rint((double)a * (double)n);
+        if (!(std::fabs(k) <= 127.0) || (float)k * invn != a)
+          return fail(KURA_ERR_UNSUPPORTED, "adjacency entry (" + std::to_string(i) + ", " + std::to_string(j) +
+                                                ") is not an integer multiple of 1/N in [-127, 127]: store it as "
+                                                "float32 (KURA_ADJ_F32)");
+        q[(size_t)i * h->ld8 + j] = (int8_t)k;
+      }
+    CU(cudaMemcpyAsync(h->adj8, q.data(), q.size(), cudaMemcpyHostToDevice, h->stream));
+  } else {
+    CU(cudaMemcpy2DAsync(h->adj, sizeof(float) * h->ld, adj, sizeof(float) * n, sizeof(float) * n, n,
+                         cudaMemcpyHostToDevice, h->stream));
+  }
   CU(cudaStreamSynchronize(h->stream));
   h->adj_set = true;
   return KURA_OK;
@@ -322,7 +354,10 @@ extern "C" int kura_generate_adjacency(kura_handle* h) {
     CU(cudaMallocAsync((void**)&bits, sizeof(uint32_t) * (size_t)words * h->n, h->stream));
     CU(kura::launch_volcano_words(h->cfg.seed, h->n, h->K, words, bits, h->stream));
   }
-  CU(kura::launch_volcano_adjacency(bits, h->n, h->K, words, h->ld, h->adj, h->stream));
+  if (h->adj8)
+    CU(kura::launch_volcano_adjacency_i8(bits, h->n, h->K, words, h->ld8, h->adj8, h->stream));
+  else
+    CU(kura::launch_volcano_adjacency(bits, h->n, h->K, words, h->ld, h->adj, h->stream));
   if (bits) CU(cudaFreeAsync(bits, h->stream));
   CU(cudaStreamSynchronize(h->stream));
   h->adj_set = true;
@@ -337,6 +372,15 @@ extern "C" int kura_get_adjacency(kura_handle* h, float* adj, int64_t n) {
   if (h->te) {
     int rc = h->te->get_adjacency(adj);
     return rc ? fail(rc, kura::TensorEngine::last_error()) : KURA_OK;
+  }
+  if (h->adj8) {
+    std::vector<int8_t> q((size_t)n * h->ld8);
+    CU(cudaMemcpyAsync(q.data(), h->adj8, q.size(), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    const float invn = 1.0f / (float)n;
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t j = 0; j < n; ++j) adj[i * n + j] = (float)q[(size_t)i * h->ld8 + j] * invn;
+    return KURA_OK;
   }
   CU(cudaMemcpy2DAsync(adj, sizeof(float) * n, h->adj, sizeof(float) * h->ld, sizeof(float) * n, n,
                        cudaMemcpyDeviceToHost, h->stream));
@@ -476,7 +520,7 @@ extern "C" int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t in
 
 static int launch(kura_handle* h, int mode, bool log_steps) {
   kura::KParams p{};
-  p.n = h->n; p.ld = h->ld; p.batch = h->B; p.k = h->K; p.coupling = h->coupling;
+  p.n = h->n; p.ld = h->ld; p.batch = h->B; p.k = h->K; p.coupling = h->adj8 ? kura::COUP_DENSE_I8 : h->coupling;
   p.dense_level = h->cfg.dense_level; p.fixed = h->cfg.fixed_step; p.rows = h->rows; p.seed = h->cfg.seed;
   p.mode = mode;
   p.omega = h->omega; p.adj = h->adj;
@@ -487,7 +531,7 @@ static int launch(kura_handle* h, int mode, bool log_steps) {
   p.out_r = h->out_r; p.out_idx = h->out_idx; p.out_theta = h->out_theta; p.out_coup = h->out_coup;
   p.ring = h->ring;
   p.log_t = h->log_t; p.log_h = h->log_h; p.log_cap = log_steps ? h->log_cap : 0;
-  p.max_attempts = -1;
+  p.max_attempts = h->launch_attempts > 0 ? h->launch_attempts : -1;
   const char* to = getenv("KURA_BARRIER_TIMEOUT_MS");
   double ms = to ? atof(to) : 20000.0;
   p.timeout_ns = (unsigned long long)(ms * 1e6);
@@ -496,6 +540,9 @@ static int launch(kura_handle* h, int mode, bool log_steps) {
   p.fin_theta = h->fin_theta; p.fin_coup = h->fin_coup;
   p.xs_smem = h->xs_smem;
   p.counters = h->counters;
+  p.adj8 = h->adj8;
+  p.ld8 = h->ld8;
+  p.invn = 1.0f / (float)h->n;
   CU(cudaMemcpyAsync(h->traj, h->htraj.data(), sizeof(TrajG) * h->B, cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(h->bar, 0, sizeof(unsigned), h->stream));
   CU(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
@@ -722,6 +769,13 @@ extern "C" int kura_rhs(kura_handle* h, int32_t traj, const float* theta, float*
   if (dtheta) CU(cudaMemcpy(dtheta, h->fin_theta + (size_t)traj * h->ld, sizeof(float) * h->n, cudaMemcpyDeviceToHost));
   if (couplings)
     CU(cudaMemcpy(couplings, h->fin_coup + (size_t)traj * 2 * h->ld, sizeof(float) * 2 * h->n, cudaMemcpyDeviceToHost));
+  return KURA_OK;
+}
+
+extern "C" int kura_set_launch_attempts(kura_handle* h, int64_t attempts) {
+  if (!h) return fail(KURA_ERR_INVALID, "handle is NULL");
+  if (h->te) return fail(KURA_ERR_UNSUPPORTED, "the tensor-core engine has no checkpoint launches");
+  h->launch_attempts = attempts > 0 ? attempts : -1;
   return KURA_OK;
 }
 

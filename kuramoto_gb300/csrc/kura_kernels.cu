@@ -49,6 +49,23 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 // streamed read of the adjacency: no L1 allocation, default L2 policy (a small A stays L2-resident)
+__device__ __forceinline__ uint2 ld_stream_u2(const int8_t* p) {
+  uint2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ uint4 ld_stream_u4(const int8_t* p) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
+// signed byte j of w as an exact float: byte ^ 0x80 placed under the exponent of 2^23
+// (0x4B000000), minus 2^23 + 128
+__device__ __forceinline__ float i8_to_f(uint32_t w_biased, int j) {
+  return __int_as_float((int)__byte_perm(w_biased, 0x4B000000u, 0x7540u + (unsigned)j)) - 8388736.0f;
+}
 __device__ __forceinline__ float4 ld_stream4(const float* p) {
   float4 v;
   asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
@@ -93,7 +110,7 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[4] = o; o += align16(sl * 4);                      // slice
   off[5] = o; o += align16(16 * 4);                      // flags
   off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
-  off[7] = o; o += align16(coup == KURA_COUPLING_DENSE ? bmax * CT * 8 : 0); // x tile
+  off[7] = o; o += align16(coup != KURA_COUPLING_VOLCANO ? bmax * (coup == COUP_DENSE_I8 && bmax == 1 ? CT_I8 : CT) * 8 : 0); // x tile
   // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
   off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
   off[9] = o; o += align16(coup == KURA_COUPLING_VOLCANO && xs_smem ? bmax * rows * 8 : 0);  // own (cos, sin)
@@ -516,6 +533,8 @@ struct Engine {
           }
         }
       }
+    } else if constexpr (COUP == COUP_DENSE_I8) {
+      dense_matvec_i8();
     } else {
       dense_matvec();
     }
@@ -596,6 +615,93 @@ struct Engine {
           }
         }
     }
+  }
+
+  static constexpr int CTX = BMAX == 1 ? CT_I8 : CT;  // columns per x tile of the int8 product
+  // one pass over RG rows per warp (rows pr0 + warp + KW*q), CPL int8 columns per lane and load
+  template <int RG, int CPL>
+  __device__ void mv_i8_pass(int pr0) {
+    constexpr int NWD = CPL / 4;
+    const int ld = p.ld, ld8 = p.ld8;
+    float acc[RG][BMAX][2];
+#pragma unroll
+    for (int q = 0; q < RG; ++q)
+#pragma unroll
+      for (int b = 0; b < BMAX; ++b) acc[q][b][0] = acc[q][b][1] = 0.f;
+    const int row0 = pr0 + warp;
+    for (int c0 = 0; c0 < ld8; c0 += CTX) {
+      __syncthreads();
+      const int cw = min(CTX, ld8 - c0);  // a multiple of 16
+      for (int t = tid; t < B * CTX; t += KT) {
+        int b = t / CTX, c = t - b * CTX;
+        xt[b * CTX + c] = (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
+      }
+      __syncthreads();
+      for (int cc = lane * CPL; cc < cw; cc += 32 * CPL) {
+        uint32_t a[RG][NWD];
+#pragma unroll
+        for (int q = 0; q < RG; ++q) {
+          const int row = row0 + KW * q;
+          const int8_t* src = p.adj8 + (size_t)row * ld8 + c0 + cc;
+          if (CPL == 16) {
+            const uint4 v = (row < r1) ? ld_stream_u4(src) : make_uint4(0u, 0u, 0u, 0u);
+            a[q][0] = v.x;
+            a[q][1 % NWD] = v.y;
+            a[q][2 % NWD] = v.z;
+            a[q][3 % NWD] = v.w;
+          } else {
+            const uint2 v = (row < r1) ? ld_stream_u2(src) : make_uint2(0u, 0u);
+            a[q][0] = v.x;
+            a[q][1 % NWD] = v.y;
+          }
+#pragma unroll
+          for (int wd = 0; wd < NWD; ++wd) a[q][wd] ^= 0x80808080u;
+        }
+#pragma unroll
+        for (int wd = 0; wd < NWD; ++wd) {
+#pragma unroll
+          for (int b = 0; b < BMAX; ++b) {
+            if (b < B) {
+              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTX + cc + 4 * wd);
+              const float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
+#pragma unroll
+              for (int q = 0; q < RG; ++q) {
+                const uint32_t w = a[q][wd];
+                const float k0 = i8_to_f(w, 0), k1 = i8_to_f(w, 1), k2 = i8_to_f(w, 2), k3 = i8_to_f(w, 3);
+                acc[q][b][0] += k0 * x01.x + k1 * x01.z + k2 * x23.x + k3 * x23.z;
+                acc[q][b][1] += k0 * x01.y + k1 * x01.w + k2 * x23.y + k3 * x23.w;
+              }
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RG; ++q)
+#pragma unroll
+      for (int b = 0; b < BMAX; ++b) {
+        acc[q][b][0] = warp_sum(acc[q][b][0]);
+        acc[q][b][1] = warp_sum(acc[q][b][1]);
+      }
+#pragma unroll
+    for (int q = 0; q < RG; ++q)
+#pragma unroll
+      for (int b = 0; b < BMAX; ++b) {
+        const int row = row0 + KW * q;
+        if (lane == (q * BMAX + b) % 32 && b < B && row < r1 && sb[b].active) {
+          float2 x = __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + row]);
+          epilogue(b, row, acc[q][b][0] * p.invn, acc[q][b][1] * p.invn, x.x, x.y);
+        }
+      }
+  }
+  // The same product with A stored as the integers N*A (int8, exact for the reference's
+  // volcano rule, K <= 127): a quarter of the HBM bytes.  Each lane streams 16 columns of
+  // 8 rows (one trajectory) or 2 rows (a batch) per load; the sums are scaled by 1/N
+  // before the epilogue.  (16 rows of 8 columns halves the shared-memory reads of x but
+  // measured 2x slower at N=65536: half the bytes in flight per load.)
+  __device__ void dense_matvec_i8() {
+    constexpr int RG = BMAX == 1 ? 8 : 2;
+    for (int pr0 = r0; pr0 < r1; pr0 += KW * RG) mv_i8_pass<RG, 16>(pr0);
   }
 
   // ---- error norm of the attempt (dp45.cu:79-84, 116-119); sum of squares -> rsum[b*PW]
@@ -934,6 +1040,9 @@ static const void* pick_kernel(int coupling, int bmax, int kmax) {
   if (coupling == KURA_COUPLING_DENSE) {
     if (bmax == 1) return kernel_ptr<KURA_COUPLING_DENSE, 1, 1>();
     if (bmax == 8) return kernel_ptr<KURA_COUPLING_DENSE, 8, 1>();
+  } else if (coupling == COUP_DENSE_I8) {
+    if (bmax == 1) return kernel_ptr<COUP_DENSE_I8, 1, 1>();
+    if (bmax == 8) return kernel_ptr<COUP_DENSE_I8, 8, 1>();
   } else {
     if (bmax == 1 && kmax == 8) return kernel_ptr<KURA_COUPLING_VOLCANO, 1, 8>();
     if (bmax == 8 && kmax == 8) return kernel_ptr<KURA_COUPLING_VOLCANO, 8, 8>();
@@ -948,7 +1057,7 @@ cudaError_t persistent_config(int coupling, int bmax, int kmax, size_t* smem_byt
   const void* f = pick_kernel(coupling, bmax, kmax);
   if (!f) return cudaErrorInvalidValue;
   int off[10], total;
-  const int kk = coupling == KURA_COUPLING_DENSE ? 1 : kmax;
+  const int kk = coupling != KURA_COUPLING_VOLCANO ? 1 : kmax;
   // keep the CTA's (cos, sin) in shared memory when it fits comfortably
   *xs_smem = 1;
   smem_layout(coupling, bmax, kk, rows_per_cta, 1, off, &total);
@@ -1041,6 +1150,31 @@ __global__ void k_volcano_adjacency(const uint32_t* __restrict__ bits, int n, in
     }
     adj[(size_t)i * ld + j] = v;
   }
+}
+// N*A as int8: kk of the row above, exact for k <= 127
+__global__ void k_volcano_adjacency_i8(const uint32_t* __restrict__ bits, int n, int k, int words, int ld8,
+                                       int8_t* __restrict__ adj8) {
+  for (int i = blockIdx.y; i < n; i += gridDim.y)
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ld8; j += gridDim.x * blockDim.x) {
+      int kk = 0;
+      if (j < n) {
+        for (int wd = 0; wd < words; ++wd) {
+          int m0 = 32 * wd, cnt = min(32, k - m0);
+          uint32_t valid = cnt >= 32 ? 0xffffffffu : ((1u << cnt) - 1u);
+          uint32_t even = 0x55555555u & valid, odd = 0xAAAAAAAAu & valid;
+          uint32_t dis = bits[(size_t)wd * n + i] ^ bits[(size_t)wd * n + j];
+          kk += __popc(even) - __popc(odd) - 2 * __popc(dis & even) + 2 * __popc(dis & odd);
+        }
+      }
+      adj8[(size_t)i * ld8 + j] = (int8_t)kk;
+    }
+}
+cudaError_t launch_volcano_adjacency_i8(const uint32_t* bits, int n, int k, int words, int ld8, int8_t* adj8,
+                                        cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  dim3 grid((unsigned)min((ld8 + 255) / 256, 64), (unsigned)min(n, 65535));
+  k_volcano_adjacency_i8<<<grid, 256, 0, st>>>(bits, n, k, words, ld8, adj8);
+  return cudaGetLastError();
 }
 cudaError_t launch_volcano_adjacency(const uint32_t* bits, int n, int k, int words, int ld, float* adj,
                                      cudaStream_t st) {

@@ -9,6 +9,7 @@ namespace kura {
 constexpr int KT = 512;       // threads per CTA of the persistent integrator
 constexpr int KW = KT / 32;   // warps per CTA
 constexpr int CT = 1024;      // columns per staged x tile of the dense coupling
+constexpr int CT_I8 = 8192;   // the same for int8 rows and one trajectory (16 loads per lane per tile)
 constexpr int PW_MAX = 2 * 32 + 2;  // partial sums per trajectory and CTA: 2K projections + (sum cos, sum sin)
 
 // Per-trajectory scalars.  Every CTA keeps an identical copy in shared memory
@@ -60,7 +61,14 @@ struct KParams {
   float* fin_theta;    // [B][ld] end-of-run phases / RHS output
   float* fin_coup;     // [B][2*ld]
   long long* counters; // [0] barriers executed (CTA 0 adds)
+  const int8_t* adj8;  // [n][ld8] N*A as int8 (dense coupling stored as integers), or null
+  int ld8;             // row stride of adj8 (a multiple of 16)
+  float invn;          // 1/N in float, the scale of adj8
 };
+
+// kernel selector for a dense adjacency stored as the integers N*A (int8); the public
+// coupling stays KURA_COUPLING_DENSE
+constexpr int COUP_DENSE_I8 = 2;
 
 enum Mode { MODE_INTEGRATE = 0, MODE_FINAL = 1, MODE_RHS = 2 };
 
@@ -71,6 +79,8 @@ cudaError_t launch_persistent(const KParams& p, int grid, int bmax, int kmax, si
 cudaError_t launch_init_state(const float* theta, int n, int ld, float* hi, float* lo, long long* w,
                               cudaStream_t st);
 cudaError_t launch_volcano_words(int seed, int n, int k, int words, uint32_t* bits, cudaStream_t st);
+cudaError_t launch_volcano_adjacency_i8(const uint32_t* bits, int n, int k, int words, int ld8, int8_t* adj8,
+                                        cudaStream_t st);
 cudaError_t launch_volcano_adjacency(const uint32_t* bits, int n, int k, int words, int ld, float* adj,
                                      cudaStream_t st);
 // sets the message returned by kura_last_error() for the calling thread

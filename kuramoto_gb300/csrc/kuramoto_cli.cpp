@@ -14,8 +14,12 @@
 // -R reloads fs.dat (theta, t, h), frequencies.dat and adj.dat when present and
 // appends to the output files, as the reference does.  The reference rewrites
 // fs.dat after every accepted step for preemption; here fs.dat is rewritten after
-// every persistent launch and at the end (set KURA_CHECKPOINT_STEPS=k to end a
-// launch at least every k accepted steps).
+// every persistent launch and at the end.  Two environment variables serve preemption:
+//   KURA_CHECKPOINT_STEPS=k  ends a launch every k step attempts, so fs.dat is rewritten
+//                            at least that often;
+//   KURA_FAIL_AT_STEP=k      host-side fault injection: once k steps are accepted, the
+//                            process exits with status 3 right after writing fs.dat, as a
+//                            preempted job would; rerunning with -R resumes from it.
 #include <cuda_runtime.h>
 #include <sys/time.h>
 #include <unistd.h>
@@ -41,6 +45,8 @@ struct Run {
   FILE* couplings = nullptr;
   FILE* times = nullptr;
   std::vector<float> floc;  // couplings last written (fs.dat checkpoint tail)
+  long long steps = 0;       // accepted steps seen by on_step
+  long long fail_at = 0;     // KURA_FAIL_AT_STEP
 };
 
 std::string path(const Run& R, const char* suffix) { return R.base + suffix; }
@@ -63,6 +69,7 @@ void write_fs(const Run& R, const float* theta, float t, float h, const float* c
 
 int on_step(void* user, int32_t, double t, double h, int64_t step) {
   Run& R = *(Run*)user;
+  R.steps = step;
   if (R.verbose) {
     double el = elapsed(R);
     double frac = (t - R.t0) / (R.t1 - R.t0);
@@ -98,6 +105,16 @@ int on_chunk(void* user, int32_t, double t, double h, const float* theta) {
   for (FILE* f : {R.order, R.thetas, R.couplings, R.times})
     if (f) fflush(f);
   if (R.dense >= 0) write_fs(R, theta, (float)t, (float)h, R.floc.data());
+  if (R.fail_at > 0 && R.steps >= R.fail_at) {
+    for (FILE* f : {R.order, R.thetas, R.couplings, R.times})
+      if (f) fclose(f);
+    FILE* out = fopen(path(R, ".out").c_str(), "ab");
+    if (out) {
+      fprintf(out, "\ninjected fault after %lld steps at t=%f\n", R.steps, t);
+      fclose(out);
+    }
+    exit(3);
+  }
   return 0;
 }
 
@@ -352,12 +369,14 @@ int main(int argc, char* argv[]) {
   }
   if (R.dense >= 2) R.couplings = fopen(path(R, "couplings.dat").c_str(), mode);
 
+  if (const char* e = getenv("KURA_CHECKPOINT_STEPS")) CHECK(kura_set_launch_attempts(H, atoll(e)));
+  if (const char* e = getenv("KURA_FAIL_AT_STEP")) R.fail_at = atoll(e);
   kura_callbacks cb;
   std::memset(&cb, 0, sizeof(cb));
   cb.user = &R;
   cb.on_output = on_output;
   cb.on_chunk = on_chunk;
-  if (R.verbose || R.dense >= 1) cb.on_step = on_step;
+  if (R.verbose || R.dense >= 1 || R.fail_at > 0) cb.on_step = on_step;
   CHECK(kura_run(H, &cb));
   for (FILE* f : {R.order, R.thetas, R.couplings, R.times})
     if (f) fclose(f);

@@ -18,6 +18,8 @@ COUPLING_VOLCANO = 1
 ENGINE_AUTO = 0
 ENGINE_PERSISTENT = 1
 ENGINE_TENSOR = 2
+ADJ_F32 = 0
+ADJ_I8 = 1
 
 ERRORS = {
     -1: "KURA_ERR_INVALID", -2: "KURA_ERR_CUDA", -3: "KURA_ERR_NOMEM", -4: "KURA_ERR_BARRIER_TIMEOUT",
@@ -36,7 +38,7 @@ class Config(ctypes.Structure):
         ("n", ctypes.c_int64), ("k", ctypes.c_int32), ("coupling", ctypes.c_int32), ("batch", ctypes.c_int32),
         ("seed", ctypes.c_int32), ("atol", ctypes.c_double), ("rtol", ctypes.c_double),
         ("fixed_step", ctypes.c_int32), ("device", ctypes.c_int32), ("dense_level", ctypes.c_int32),
-        ("engine", ctypes.c_int32), ("stream", ctypes.c_void_p),
+        ("engine", ctypes.c_int32), ("stream", ctypes.c_void_p), ("adj_storage", ctypes.c_int32),
     ]
 
 
@@ -115,6 +117,7 @@ def lib():
         "kura_final_record": (i32, [P, i32, fp, fp, ctypes.POINTER(f64), ctypes.POINTER(f64)]),
         "kura_rhs": (i32, [P, i32, fp, fp, fp]),
         "kura_get_stats": (i32, [P, ctypes.POINTER(Stats)]),
+        "kura_set_launch_attempts": (i32, [P, i64]),
         "kura_random_inputs": (i32, [i32, i64, ctypes.c_float, ctypes.c_float, i32, i32, i32, fp, fp]),
         "kura_volcano_factor": (i32, [i32, i64, i32, ctypes.c_void_p]),
         "kura_multi_create": (i32, [ctypes.POINTER(Instance), i32, f64, f64, f64, f64, f64, i32, i32, i32,
@@ -167,9 +170,10 @@ def volcano_factor(seed, n, k):
 
 class Network:
     def __init__(self, n, k=6, coupling=COUPLING_DENSE, batch=1, seed=1, atol=1e-6, rtol=0.0, fixed_step=False,
-                 device=0, dense_level=0, stream=None, engine=0):
+                 device=0, dense_level=0, stream=None, engine=0, adj_storage=ADJ_F32):
         c = Config()
         c.n, c.k, c.coupling, c.batch, c.seed, c.engine = n, k, coupling, batch, seed, engine
+        c.adj_storage = adj_storage
         c.atol, c.rtol, c.fixed_step, c.device, c.dense_level = atol, rtol, int(fixed_step), device, dense_level
         c.stream = stream
         self.cfg = c
@@ -181,9 +185,10 @@ class Network:
         self.h = h
 
     @staticmethod
-    def memory_required(n, k=6, coupling=COUPLING_DENSE, batch=1, dense_level=0, engine=0):
+    def memory_required(n, k=6, coupling=COUPLING_DENSE, batch=1, dense_level=0, engine=0, adj_storage=ADJ_F32):
         c = Config()
         c.n, c.k, c.coupling, c.batch, c.atol, c.dense_level, c.engine = n, k, coupling, batch, 1e-6, dense_level, engine
+        c.adj_storage = adj_storage
         b = ctypes.c_int64()
         _check(lib().kura_memory_required(ctypes.byref(c), ctypes.byref(b)))
         return b.value
@@ -287,6 +292,9 @@ class Network:
         cp = np.zeros(2 * self.n, np.float32)
         _check(lib().kura_rhs(self.h, traj, _fptr(th), _fptr(f), _fptr(cp)))
         return f, cp
+
+    def set_launch_attempts(self, attempts):
+        _check(lib().kura_set_launch_attempts(self.h, attempts))
 
     def stats(self):
         s = Stats()

@@ -117,3 +117,40 @@ def test_fixed_step_cli(native, oracle_lib, tmp_path):
     g, c = res["gpu"][0], res["cpu"][0]
     assert load(g, "times.dat").size == load(c, "times.dat").size == 4
     assert np.max(np.abs(load(g, "order.dat") - load(c, "order.dat"))) < 1e-3
+
+
+@pytest.mark.parametrize("volcano", [False, True])
+def test_fault_injection_resume(native, tmp_path, volcano):
+    """Preemption and resume without a GPU fault: KURA_FAIL_AT_STEP makes the host process
+    exit(3) right after it rewrites fs.dat; rerunning with -R continues from fs.dat and
+    appends.  The result matches an uninterrupted run to the float32 checkpoint precision
+    (fs.dat stores theta, t and h as float32, as the reference does)."""
+    n = 1500
+    args = ["-N", str(n), "-K", "5", "-c", "3", "-t", "30", "-d", "1", "-D", "1", "-n", "-s", "4"]
+    if volcano:
+        args.append("-A")
+    full = str(tmp_path / "full")
+    r = subprocess.run([native.cli_path(), *args, full], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    cut = str(tmp_path / "cut")
+    env = dict(os.environ, KURA_CHECKPOINT_STEPS="40", KURA_FAIL_AT_STEP="100")
+    r = subprocess.run([native.cli_path(), *args, cut], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 3, (r.returncode, r.stdout, r.stderr)
+    assert "injected fault after" in open(cut + ".out").read()
+    fs = np.fromfile(cut + "fs.dat", np.float32)
+    t_chk = float(fs[n])
+    assert fs.size == 3 * n + 2 and 0 < t_chk < 30
+    part = load(cut, "order.dat")
+    assert 1 <= part.size < 31
+    r = subprocess.run([native.cli_path(), *args, "-R", cut], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    a, b = load(full, "order.dat"), load(cut, "order.dat")
+    assert a.size == b.size == 31
+    assert np.max(np.abs(a - b)) < 1e-4, np.max(np.abs(a - b))
+    ta, tb = load(full, "thetas.dat").reshape(-1, n), load(cut, "thetas.dat").reshape(-1, n)
+    assert ta.shape == tb.shape
+    assert np.max(np.abs(ta - tb) - 4 * np.spacing(np.abs(ta))) < 1e-4
+    # the step times: the interrupted run's up to the checkpoint, then the resumed run's
+    sa, sb = load(full, "times.dat"), load(cut, "times.dat")
+    assert abs(sa.size - sb.size) <= 3
+    assert np.all(np.diff(sb) > 0) and sb[-1] >= 30.0
