@@ -74,6 +74,13 @@ struct kura_handle {
   std::vector<double> t0;
   bool omega_set = false, adj_set = false, horizon_set = false;
   long long launch_attempts = -1;  // step attempts per persistent launch (< 0: unbounded)
+  // pinned host memory: the trajectory states and error flag of a launch in flight, and the
+  // staging area its records are copied to while the next launch runs
+  TrajG* traj_pin = nullptr;
+  int* err_h = nullptr;
+  char* stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaEvent_t ev_stage = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   kura_stats stats{};
   kura::TensorEngine* te = nullptr;  // the tensor-core ensemble, when selected
@@ -160,6 +167,10 @@ extern "C" void kura_destroy(kura_handle* h) {
     if (p) cudaFree(p);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->ev_stage) cudaEventDestroy(h->ev_stage);
+  if (h->traj_pin) cudaFreeHost(h->traj_pin);
+  if (h->err_h) cudaFreeHost(h->err_h);
+  if (h->stage) cudaFreeHost(h->stage);
   delete h->te;
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -266,6 +277,9 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   h->log_cap = 4096;
   CUH(dalloc(&h->log_t, B * (size_t)h->log_cap));
   CUH(dalloc(&h->log_h, B * (size_t)h->log_cap));
+  CUH(cudaMallocHost((void**)&h->traj_pin, sizeof(TrajG) * B));
+  CUH(cudaMallocHost((void**)&h->err_h, sizeof(int)));
+  CUH(cudaEventCreateWithFlags(&h->ev_stage, cudaEventDisableTiming));
   h->htraj.assign(B, TrajG{});
   for (auto& T : h->htraj) {
     T.status = 1;  // no state yet
@@ -518,7 +532,8 @@ extern "C" int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t in
   return KURA_OK;
 }
 
-static int launch(kura_handle* h, int mode, bool log_steps) {
+// enqueues one persistent launch (state upload, kernel, error flag and state download)
+static int launch_begin(kura_handle* h, int mode, bool log_steps) {
   kura::KParams p{};
   p.n = h->n; p.ld = h->ld; p.batch = h->B; p.k = h->K; p.coupling = h->adj8 ? kura::COUP_DENSE_I8 : h->coupling;
   p.dense_level = h->cfg.dense_level; p.fixed = h->cfg.fixed_step; p.rows = h->rows; p.seed = h->cfg.seed;
@@ -543,22 +558,32 @@ static int launch(kura_handle* h, int mode, bool log_steps) {
   p.adj8 = h->adj8;
   p.ld8 = h->ld8;
   p.invn = 1.0f / (float)h->n;
-  CU(cudaMemcpyAsync(h->traj, h->htraj.data(), sizeof(TrajG) * h->B, cudaMemcpyHostToDevice, h->stream));
+  std::memcpy(h->traj_pin, h->htraj.data(), sizeof(TrajG) * h->B);
+  CU(cudaMemcpyAsync(h->traj, h->traj_pin, sizeof(TrajG) * h->B, cudaMemcpyHostToDevice, h->stream));
   CU(cudaMemsetAsync(h->bar, 0, sizeof(unsigned), h->stream));
   CU(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
   CU(cudaEventRecord(h->ev0, h->stream));
   CU(kura::launch_persistent(p, h->grid, h->bmax, h->kmax, h->smem, h->stream));
   CU(cudaEventRecord(h->ev1, h->stream));
-  int err = 0;
-  CU(cudaMemcpyAsync(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  CU(cudaMemcpyAsync(h->htraj.data(), h->traj, sizeof(TrajG) * h->B, cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(h->err_h, h->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaMemcpyAsync(h->traj_pin, h->traj, sizeof(TrajG) * h->B, cudaMemcpyDeviceToHost, h->stream));
+  return KURA_OK;
+}
+// waits for the launch enqueued by launch_begin
+static int launch_end(kura_handle* h) {
   CU(cudaStreamSynchronize(h->stream));
+  std::memcpy(h->htraj.data(), h->traj_pin, sizeof(TrajG) * h->B);
   float ms_k = 0;
   CU(cudaEventElapsedTime(&ms_k, h->ev0, h->ev1));
   h->stats.kernel_ms += ms_k;
   h->stats.launches++;
+  const int err = *h->err_h;
   if (err) return fail(err, err == KURA_ERR_BARRIER_TIMEOUT ? "grid barrier timed out" : "persistent kernel aborted");
   return KURA_OK;
+}
+static int launch(kura_handle* h, int mode, bool log_steps) {
+  int rc = launch_begin(h, mode, log_steps);
+  return rc ? rc : launch_end(h);
 }
 
 extern "C" int kura_run(kura_handle* h, const kura_callbacks* cb) {
@@ -606,88 +631,142 @@ extern "C" int kura_run(kura_handle* h, const kura_callbacks* cb) {
     return KURA_OK;
   }
   const bool log_steps = cb && cb->on_step;
-  std::vector<float> rbuf, thbuf, cpbuf;
-  std::vector<int> ibuf;
-  std::vector<double> lt, lh;
+  const bool want_out = cb && cb->on_output, want_chunk = cb && cb->on_chunk;
+  const int dl = h->cfg.dense_level;
   std::vector<long long> step_no(h->B, 0);
   for (int b = 0; b < h->B; ++b) step_no[b] = h->htraj[b].accepted;
+  // Records of launch k are copied into pinned staging memory on the stream, launch k+1 is
+  // enqueued behind the copies, and the observers consume launch k's records while k+1 runs.
+  struct Seg {
+    size_t r, idx, th, cp, lt, lh, chunk;
+    int cnt, logs;
+  };
+  std::vector<Seg> seg(h->B);
+  auto progress = [&]() {
+    long long v = 0;
+    for (auto& T : h->htraj) v += T.accepted + T.rejected + T.eval_i;
+    return v;
+  };
+  int rc = launch(h, kura::MODE_INTEGRATE, log_steps);
+  if (rc) return rc;
+  long long before = 0;
   int stall = 0;
   while (true) {
-    long long before = 0;
-    for (auto& T : h->htraj) before += T.accepted + T.rejected + T.out_count + T.eval_i;
-    int rc = launch(h, kura::MODE_INTEGRATE, log_steps);
-    if (rc) return rc;
-    // drain (order.dat, thetas.dat, couplings.dat, times.dat records)
+    // ---- stage the records of the launch that just ended
+    size_t need = 0;
+    auto take = [&](size_t bytes) {
+      size_t o = need;
+      need += (bytes + 255) / 256 * 256;
+      return o;
+    };
     for (int b = 0; b < h->B; ++b) {
-      TrajG& T = h->htraj[b];
-      int cnt = T.out_count;
-      if (cnt > 0) {
-        rbuf.resize(cnt);
-        ibuf.resize(cnt);
-        CU(cudaMemcpy(rbuf.data(), h->out_r + (size_t)b * h->ring, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(ibuf.data(), h->out_idx + (size_t)b * h->ring, sizeof(int) * cnt, cudaMemcpyDeviceToHost));
-        for (int q = 0; q < cnt; ++q) h->order[b].push_back(rbuf[q]);
-        if (cb && cb->on_output) {
-          int dl = h->cfg.dense_level;
-          if (dl >= 1) {
-            thbuf.resize((size_t)cnt * h->ld);
-            CU(cudaMemcpy(thbuf.data(), h->out_theta + (size_t)b * h->ring * h->ld, sizeof(float) * cnt * h->ld,
-                          cudaMemcpyDeviceToHost));
-          }
-          if (dl >= 2) {
-            cpbuf.resize((size_t)cnt * 2 * h->ld);
-            CU(cudaMemcpy(cpbuf.data(), h->out_coup + (size_t)b * h->ring * 2 * h->ld,
-                          sizeof(float) * cnt * 2 * h->ld, cudaMemcpyDeviceToHost));
-          }
-          for (int q = 0; q < cnt; ++q) {
-            int idx = ibuf[q];
-            double te = idx < 0 ? h->t0[b] : (double)h->t_eval_h[idx];
-            const float* th = dl >= 1 ? thbuf.data() + (size_t)q * h->ld : nullptr;
-            const float* cp = dl >= 2 ? cpbuf.data() + (size_t)q * 2 * h->ld : nullptr;
-            if (cb->on_output(cb->user, b, idx, te, rbuf[q], th, cp)) return fail(KURA_ERR_CALLBACK, "on_output aborted");
-          }
-        }
-      }
-      if (log_steps && T.log_count > 0) {
-        int lc = std::min(T.log_count, h->log_cap);
-        lt.resize(lc);
-        lh.resize(lc);
-        CU(cudaMemcpy(lt.data(), h->log_t + (size_t)b * h->log_cap, sizeof(double) * lc, cudaMemcpyDeviceToHost));
-        CU(cudaMemcpy(lh.data(), h->log_h + (size_t)b * h->log_cap, sizeof(double) * lc, cudaMemcpyDeviceToHost));
-        for (int q = 0; q < lc; ++q)
-          if (cb->on_step(cb->user, b, lt[q], lh[q], ++step_no[b])) return fail(KURA_ERR_CALLBACK, "on_step aborted");
-      }
-      T.out_count = 0;
-      T.log_count = 0;
+      const TrajG& T = h->htraj[b];
+      Seg& S = seg[b];
+      S.cnt = T.out_count;
+      S.logs = log_steps ? std::min(T.log_count, h->log_cap) : 0;
+      S.r = take(sizeof(float) * S.cnt);
+      S.idx = take(sizeof(int) * S.cnt);
+      S.th = take(want_out && dl >= 1 ? sizeof(float) * S.cnt * h->ld : 0);
+      S.cp = take(want_out && dl >= 2 ? sizeof(float) * S.cnt * 2 * h->ld : 0);
+      S.lt = take(sizeof(double) * S.logs);
+      S.lh = take(sizeof(double) * S.logs);
+      S.chunk = take(want_chunk ? sizeof(float) * h->n : 0);
     }
-    if (cb && cb->on_chunk) {
-      thbuf.resize(h->ld);
-      for (int b = 0; b < h->B; ++b) {
-        const TrajG& T = h->htraj[b];
+    if (need > h->stage_bytes) {
+      if (h->stage) CU(cudaFreeHost(h->stage));
+      h->stage = nullptr;
+      h->stage_bytes = 0;
+      CU(cudaMallocHost((void**)&h->stage, need));
+      h->stage_bytes = need;
+    }
+    char* st = h->stage;
+    for (int b = 0; b < h->B; ++b) {
+      const TrajG& T = h->htraj[b];
+      const Seg& S = seg[b];
+      if (S.cnt > 0) {
+        CU(cudaMemcpyAsync(st + S.r, h->out_r + (size_t)b * h->ring, sizeof(float) * S.cnt, cudaMemcpyDeviceToHost,
+                           h->stream));
+        CU(cudaMemcpyAsync(st + S.idx, h->out_idx + (size_t)b * h->ring, sizeof(int) * S.cnt, cudaMemcpyDeviceToHost,
+                           h->stream));
+        if (want_out && dl >= 1)
+          CU(cudaMemcpyAsync(st + S.th, h->out_theta + (size_t)b * h->ring * h->ld, sizeof(float) * S.cnt * h->ld,
+                             cudaMemcpyDeviceToHost, h->stream));
+        if (want_out && dl >= 2)
+          CU(cudaMemcpyAsync(st + S.cp, h->out_coup + (size_t)b * h->ring * 2 * h->ld,
+                             sizeof(float) * S.cnt * 2 * h->ld, cudaMemcpyDeviceToHost, h->stream));
+      }
+      if (S.logs > 0) {
+        CU(cudaMemcpyAsync(st + S.lt, h->log_t + (size_t)b * h->log_cap, sizeof(double) * S.logs,
+                           cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaMemcpyAsync(st + S.lh, h->log_h + (size_t)b * h->log_cap, sizeof(double) * S.logs,
+                           cudaMemcpyDeviceToHost, h->stream));
+      }
+      if (want_chunk) {
         size_t off = ((size_t)T.rot_y * h->B + b) * h->ld;
         CU(kura::launch_unwrap(h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->n, h->fin_theta + (size_t)b * h->ld,
                                h->stream));
-        CU(cudaMemcpyAsync(thbuf.data(), h->fin_theta + (size_t)b * h->ld, sizeof(float) * h->n,
+        CU(cudaMemcpyAsync(st + S.chunk, h->fin_theta + (size_t)b * h->ld, sizeof(float) * h->n,
                            cudaMemcpyDeviceToHost, h->stream));
-        CU(cudaStreamSynchronize(h->stream));
-        if (cb->on_chunk(cb->user, b, T.t, T.h, thbuf.data())) return fail(KURA_ERR_CALLBACK, "on_chunk aborted");
       }
     }
+    CU(cudaEventRecord(h->ev_stage, h->stream));
+    std::vector<double> chunk_t(h->B), chunk_h(h->B);
     bool done = true;
     int errc = 0;
-    for (auto& T : h->htraj) {
+    for (int b = 0; b < h->B; ++b) {
+      TrajG& T = h->htraj[b];
+      chunk_t[b] = T.t;
+      chunk_h[b] = T.h;
+      T.out_count = 0;
+      T.log_count = 0;
       if (T.status == 0 || T.eval_i < T.eval_end) done = false;
       if (T.status < 0 && !errc) errc = T.status;
     }
-    long long after = 0;
-    for (auto& T : h->htraj) after += T.accepted + T.rejected + T.eval_i;
+    const long long after = progress();
+    stall = (after == before) ? stall + 1 : 0;
+    before = after;
+    // ---- the next launch runs while the observers read the staged records
+    bool running = false;
+    if (!done && !errc && stall <= 2) {
+      rc = launch_begin(h, kura::MODE_INTEGRATE, log_steps);
+      if (rc) return rc;
+      running = true;
+    }
+    CU(cudaEventSynchronize(h->ev_stage));
+    int abort = 0;
+    for (int b = 0; b < h->B && !abort; ++b) {
+      const Seg& S = seg[b];
+      const float* r = (const float*)(st + S.r);
+      const int* idx = (const int*)(st + S.idx);
+      for (int q = 0; q < S.cnt; ++q) h->order[b].push_back(r[q]);
+      if (want_out) {
+        for (int q = 0; q < S.cnt && !abort; ++q) {
+          const double te = idx[q] < 0 ? h->t0[b] : (double)h->t_eval_h[idx[q]];
+          const float* th = dl >= 1 ? (const float*)(st + S.th) + (size_t)q * h->ld : nullptr;
+          const float* cp = dl >= 2 ? (const float*)(st + S.cp) + (size_t)q * 2 * h->ld : nullptr;
+          if (cb->on_output(cb->user, b, idx[q], te, r[q], th, cp)) abort = 1;
+        }
+      }
+      const double* lt = (const double*)(st + S.lt);
+      const double* lh = (const double*)(st + S.lh);
+      for (int q = 0; q < S.logs && !abort; ++q)
+        if (cb->on_step(cb->user, b, lt[q], lh[q], ++step_no[b])) abort = 2;
+    }
+    if (want_chunk)
+      for (int b = 0; b < h->B && !abort; ++b)
+        if (cb->on_chunk(cb->user, b, chunk_t[b], chunk_h[b], (const float*)(st + seg[b].chunk))) abort = 3;
+    if (running) {
+      rc = launch_end(h);
+      if (rc) return rc;
+    }
+    if (abort) return fail(KURA_ERR_CALLBACK, abort == 1 ? "on_output aborted" : abort == 2 ? "on_step aborted"
+                                                                                          : "on_chunk aborted");
     if (errc) {
       const char* m = errc == KURA_ERR_STEP_UNDERFLOW ? "step size underflow" : "non-finite error norm";
       return fail(errc, m);
     }
     if (done) break;
-    stall = (after == before) ? stall + 1 : 0;
-    if (stall > 2) return fail(KURA_ERR_INVALID, "integration made no progress");
+    if (!running) return fail(KURA_ERR_INVALID, "integration made no progress");
   }
   long long acc = 0, rej = 0, bars = 0;
   for (auto& T : h->htraj) { acc += T.accepted; rej += T.rejected; }

@@ -270,3 +270,42 @@ def test_barrier_timeout_reports_error_and_context_survives(native, monkeypatch)
     net.run()
     assert net.order(0).size == 2
     net.close()
+
+
+@pytest.mark.parametrize("coupling", [DENSE, VOLCANO])
+def test_checkpointed_launches_are_bitwise_identical(native, coupling):
+    """A run cut into many launches (a checkpoint every 7 attempts, records drained while
+    the next launch runs) gives bitwise the records of a single launch: the whole state
+    stays on the device between launches."""
+    n, batch = 700, 3
+    th, om = normal_inputs(n, 12, init=2 * np.pi)
+    runs = []
+    for attempts in (0, 7):
+        net = make(native, n, 5, coupling, th, om, c=3.0, batch=batch, dense_level=2, t1=6.0, dt=0.5,
+                   cs=[1.5, 3.0, 4.5], thetas=[th, th + 0.1, th + 0.2])
+        if attempts:
+            net.set_launch_attempts(attempts)
+        chunks = []
+        rec = {b: [] for b in range(batch)}
+        steps = {b: [] for b in range(batch)}
+        net.run(on_output=lambda b, i, t, r, theta, cp: rec[b].append((i, t, r, theta, cp)) and False,
+                on_step=lambda b, t, h, s: steps[b].append((t, h, s)) and False,
+                on_chunk=lambda b, t, h, theta: chunks.append((b, t, h, theta)) and False)
+        runs.append((rec, steps, chunks, net.stats(), [net.order(b) for b in range(batch)]))
+        net.close()
+    (r1, s1, c1, st1, o1), (r2, s2, c2, st2, o2) = runs
+    assert st1["launches"] == 1 and st2["launches"] > 5
+    assert st1["accepted"] == st2["accepted"]
+    for b in range(batch):
+        assert s1[b] == s2[b]
+        assert len(r1[b]) == len(r2[b]) == 13
+        for x, y in zip(r1[b], r2[b]):
+            assert x[:3] == y[:3]
+            assert np.array_equal(x[3], y[3]) and np.array_equal(x[4], y[4])
+        assert np.array_equal(o1[b], o2[b])
+    assert len(c2) == batch * st2["launches"] and len(c1) == batch
+    # the last checkpoint of the cut run is the state of the single launch's end
+    for b in range(batch):
+        last1 = [c for c in c1 if c[0] == b][-1]
+        last2 = [c for c in c2 if c[0] == b][-1]
+        assert last1[1] == last2[1] and np.array_equal(last1[3], last2[3])
