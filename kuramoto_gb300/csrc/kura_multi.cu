@@ -69,7 +69,17 @@ struct MParams {
   long long* accepted;  // by MInst::id
   long long* rejected;
   int* status;             // by MInst::id: 1 done, < 0 a KURA_ERR_* code
-  long long max_attempts;  // < 0: unbounded (the autotuner's samples bound it)
+  long long max_attempts;  // per network and launch, < 0: unbounded
+  struct MNet* state;      // by MInst::id: the controller state between launches
+};
+
+// A network's controller between launches: a launch that stops a network after
+// max_attempts leaves it here, and the next launch resumes it (the phases and slopes stay
+// in HBM).  stage: 0 not started, 1 resumable, 2 finished.
+struct MNet {
+  double t, h, t_last;
+  long long acc, rej;
+  int rot_y, rot_g, eval_i, eval_end, status, stage;
 };
 
 struct MSmem {
@@ -205,14 +215,16 @@ struct Multi {
         p.ph_w[(base ^ 1) * T + gi] = w7;
       }
       if (proj) {
-        // u_m = -1 flips the sign bit: sum_n u_mn (cos_n, sin_n); slots m >= k stay unused
+        // u_m = -1 flips the sign bit: sum_n u_mn (cos_n, sin_n)
         const uint32_t nu = ~(uint32_t)ubits[i - r0];
         const uint32_t cb = __float_as_uint(cs), sb = __float_as_uint(sn);
 #pragma unroll
         for (int m = 0; m < M_KMAX; ++m) {
-          const uint32_t sg = (nu << (31 - m)) & 0x80000000u;
-          acc[2 * m] += __uint_as_float(cb ^ sg);
-          acc[2 * m + 1] += __uint_as_float(sb ^ sg);
+          if (m < k) {  // uniform over the cluster: the rank of the network
+            const uint32_t sg = (nu << (31 - m)) & 0x80000000u;
+            acc[2 * m] += __uint_as_float(cb ^ sg);
+            acc[2 * m + 1] += __uint_as_float(sb ^ sg);
+          }
         }
       }
       if (want_r) {
@@ -259,34 +271,55 @@ struct Multi {
     const int R = (n + CS - 1) / CS;
     r0 = min(n, rank * R);
     r1 = min(n, r0 + R);
-    // factor bits (low bit of Philox element m*N + i, kuramoto.cu:128-135) and y(0)
+    MNet& G = p.state[I.id];
+    const int stage = G.stage;  // the same on every CTA of the cluster
+    if (stage == 2) return;     // finished by an earlier launch
+    // factor bits (low bit of Philox element m*N + i, kuramoto.cu:128-135) and, on a fresh
+    // start, y(0)
     for (int i = r0 + tid; i < r1; i += NT) {
       uint32_t w = 0;
       for (int m = 0; m < k; ++m)
         w |= (stream_word(I.seed, (unsigned long long)m * (unsigned long long)n + (unsigned long long)i) & 1u) << m;
       ubits[i - r0] = (uint8_t)w;
-      const double th = (double)p.theta0[off + i];
-      const double kk = rint(th / TWO_PI_D);
-      const double rr = th - kk * TWO_PI_D;
-      const float hi = (float)rr;
-      p.ph_hi[off + i] = hi;
-      p.ph_lo[off + i] = (float)(rr - (double)hi);
-      p.ph_w[off + i] = (long long)kk;
+      if (stage == 0) {
+        const double th = (double)p.theta0[off + i];
+        const double kk = rint(th / TWO_PI_D);
+        const double rr = th - kk * TWO_PI_D;
+        const float hi = (float)rr;
+        p.ph_hi[off + i] = hi;
+        p.ph_lo[off + i] = (float)(rr - (double)hi);
+        p.ph_w[off + i] = (long long)kk;
+      }
     }
     if (tid == 0) {
-      S.t = 0.0;
-      S.h = p.h0;
-      S.t_last = 0.0;
-      S.acc = S.rej = 0;
-      S.rot_y = S.rot_g = 0;
-      S.eval_i = S.eval_end = 0;
-      S.status = 0;
+      if (stage == 0) {
+        S.t = 0.0;
+        S.h = p.h0;
+        S.t_last = 0.0;
+        S.acc = S.rej = 0;
+        S.rot_y = S.rot_g = 0;
+        S.eval_i = S.eval_end = 0;
+        S.status = 0;
+      } else {
+        S.t = G.t;
+        S.h = G.h;
+        S.t_last = G.t_last;
+        S.acc = G.acc;
+        S.rej = G.rej;
+        S.rot_y = G.rot_y;
+        S.rot_g = G.rot_g;
+        S.eval_i = G.eval_i;
+        S.eval_end = G.eval_end;
+        S.status = G.status;
+      }
       S.mh = S.ml = 0.f;
     }
     __syncthreads();
-    // first slope of the run (dp45.cu:151) and the record at t = 0
-    coupling(0, 0, 0, 0, true, false);
-    record(I, 0);
+    if (stage == 0) {
+      // first slope of the run (dp45.cu:151) and the record at t = 0
+      coupling(0, 0, 0, 0, true, false);
+      record(I, 0);
+    }
     long long attempts = 0;
     const long long T = p.total;
     while (true) {
@@ -379,15 +412,29 @@ struct Multi {
       }
       __syncthreads();
     }
-    if (p.theta_out)
+    const bool finished = !(S.t < p.t1) || S.status != 0;
+    if (p.theta_out && finished)
       for (int i = r0 + tid; i < r1; i += NT) {
         const long long a = S.rot_y * T + off + i;
         p.theta_out[off + i] = (float)((double)p.ph_w[a] * TWO_PI_D + (double)p.ph_hi[a] + (double)p.ph_lo[a]);
       }
+    // every CTA has read G.stage and S before rank 0 rewrites the state
+    cl.sync();
     if (rank == 0 && tid == 0) {
+      G.t = S.t;
+      G.h = S.h;
+      G.t_last = S.t_last;
+      G.acc = S.acc;
+      G.rej = S.rej;
+      G.rot_y = S.rot_y;
+      G.rot_g = S.rot_g;
+      G.eval_i = S.eval_i;
+      G.eval_end = S.eval_end;
+      G.status = S.status;
+      G.stage = finished ? 2 : 1;
       p.accepted[I.id] = S.acc;
       p.rejected[I.id] = S.rej;
-      p.status[I.id] = S.status == 0 ? 1 : S.status;
+      p.status[I.id] = finished ? (S.status == 0 ? 1 : S.status) : 0;
     }
   }
 
@@ -476,7 +523,11 @@ struct kura_multi {
   float *d_om = nullptr, *d_th = nullptr, *d_hi = nullptr, *d_lo = nullptr, *d_g = nullptr, *d_r = nullptr,
         *d_theta = nullptr;
   long long *d_w = nullptr, *d_acc = nullptr, *d_rej = nullptr;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;   // pilot: every network's first attempts, in size order
+  cudaGraphExec_t graph2 = nullptr;  // the rest, longest predicted work first
+  kura::MNet* d_state = nullptr;
+  MInst* d_inst2 = nullptr;
+  int pilot_attempts = 32;
   kura_multi_stats stats = {};
 };
 
@@ -519,6 +570,7 @@ MParams base_params(kura_multi* m) {
   p.rejected = m->d_rej;
   p.status = m->d_status;
   p.max_attempts = -1;
+  p.state = m->d_state;
   return p;
 }
 
@@ -549,6 +601,7 @@ int autotune(kura_multi* m) {
     for (int t : nts) {
       if (m->want_nt > 0 && t != m->want_nt) continue;
       MCU(cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->st));
+      MCU(cudaMemsetAsync(m->d_state, 0, sizeof(kura::MNet) * S, m->st));
       MCU(cudaEventRecord(m->ev[0], m->st));
       cudaError_t e = kura::launch_multi(q, c, t, m->st, nullptr);
       if (e != cudaSuccess) {
@@ -578,25 +631,42 @@ int autotune(kura_multi* m) {
   return KURA_OK;
 }
 
+cudaError_t capture(kura_multi* m, const MParams& p, bool reset_state, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t e1 = cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->st);
+  if (e1 == cudaSuccess && reset_state) e1 = cudaMemsetAsync(m->d_state, 0, sizeof(kura::MNet) * m->count, m->st);
+  cudaError_t e2 = e1 == cudaSuccess ? kura::launch_multi(p, m->cs, m->nt, m->st, &m->grid) : e1;
+  cudaError_t e3 = cudaStreamEndCapture(m->st, &g);
+  if (e2 != cudaSuccess || e3 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return e2 != cudaSuccess ? e2 : e3;
+  }
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  return e;
+}
+
+// two launches per integration: a pilot runs the first attempts of every network (largest
+// first); the host then orders the unfinished networks by their predicted remaining work,
+// (t1 - t) / h steps of (N + 2048) row-equivalents each, and the second launch runs them in
+// that order, so the networks with the most steps start first (longest-processing-time)
 int build_graph(kura_multi* m) {
   MParams p = base_params(m);
   p.rows_max = (m->maxn + m->cs - 1) / m->cs;
   MCU(cudaMemcpyAsync(m->d_inst, m->queue.data(), sizeof(MInst) * m->count, cudaMemcpyHostToDevice, m->st));
   MCU(cudaStreamSynchronize(m->st));
-  cudaGraph_t g = nullptr;
-  MCU(cudaStreamBeginCapture(m->st, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e1 = cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->st);
-  cudaError_t e2 = kura::launch_multi(p, m->cs, m->nt, m->st, &m->grid);
-  cudaError_t e3 = cudaStreamEndCapture(m->st, &g);
-  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
-    if (g) cudaGraphDestroy(g);
-    cudaGetLastError();
-    return mfail(KURA_ERR_CUDA, std::string("capturing the multi-network launch: ") +
-                                    cudaGetErrorString(e2 != cudaSuccess ? e2 : (e1 != cudaSuccess ? e1 : e3)));
+  p.max_attempts = m->pilot_attempts;
+  cudaError_t e = capture(m, p, true, &m->graph);
+  if (e == cudaSuccess) {
+    p.max_attempts = -1;
+    p.inst = m->d_inst2;
+    e = capture(m, p, false, &m->graph2);
   }
-  cudaError_t e4 = cudaGraphInstantiate(&m->graph, g, 0);
-  cudaGraphDestroy(g);
-  MCU(e4);
+  if (e != cudaSuccess)
+    return mfail(KURA_ERR_CUDA, std::string("capturing the multi-network launches: ") + cudaGetErrorString(e));
   return KURA_OK;
 }
 
@@ -678,6 +748,7 @@ extern "C" int kura_multi_create(const kura_instance* inst, int32_t count, doubl
       {(void**)&m->d_g, sizeof(float) * 7 * T},    {(void**)&m->d_r, sizeof(float) * rec},
       {(void**)&m->d_theta, sizeof(float) * T},    {(void**)&m->d_acc, sizeof(long long) * count},
       {(void**)&m->d_rej, sizeof(long long) * count},
+      {(void**)&m->d_state, sizeof(kura::MNet) * count}, {(void**)&m->d_inst2, sizeof(MInst) * count},
   };
   for (auto& a : allocs) {
     e = cudaMalloc(a.p, a.bytes);
@@ -698,8 +769,10 @@ extern "C" void kura_multi_destroy(kura_multi* m) {
   cudaSetDevice(m->device);
   if (m->st) cudaStreamSynchronize(m->st);
   if (m->graph) cudaGraphExecDestroy(m->graph);
-  void* ptrs[] = {m->d_inst, m->d_queue, m->d_status, m->d_om, m->d_th, m->d_hi, m->d_lo,
-                  m->d_w,    m->d_g,     m->d_r,      m->d_theta, m->d_acc, m->d_rej};
+  if (m->graph2) cudaGraphExecDestroy(m->graph2);
+  void* ptrs[] = {m->d_inst, m->d_queue, m->d_status, m->d_om,    m->d_th,    m->d_hi,    m->d_lo,
+                  m->d_w,    m->d_g,     m->d_r,      m->d_theta, m->d_acc,   m->d_rej,   m->d_state,
+                  m->d_inst2};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t v : m->ev)
@@ -732,6 +805,24 @@ extern "C" int kura_multi_integrate(kura_multi* m, const float* omega, const flo
   }
   MCU(cudaEventRecord(m->ev[0], m->st));
   MCU(cudaGraphLaunch(m->graph, m->st));
+  std::vector<kura::MNet> state(m->count);
+  MCU(cudaMemcpyAsync(state.data(), m->d_state, sizeof(kura::MNet) * m->count, cudaMemcpyDeviceToHost, m->st));
+  MCU(cudaStreamSynchronize(m->st));
+  std::vector<std::pair<double, int>> cost;
+  cost.reserve(m->count);
+  for (int q = 0; q < m->count; ++q) {
+    const MInst& I = m->queue[q];
+    const kura::MNet& G = state[I.id];
+    const double steps = G.stage == 2 ? 0.0 : std::max(0.0, m->t1 - G.t) / std::max(G.h, 1e-300);
+    cost.push_back({steps * ((double)I.n + 2048.0), q});
+  }
+  std::stable_sort(cost.begin(), cost.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+    return a.first > b.first;
+  });
+  std::vector<MInst> order2(m->count);
+  for (int q = 0; q < m->count; ++q) order2[q] = m->queue[cost[q].second];
+  MCU(cudaMemcpyAsync(m->d_inst2, order2.data(), sizeof(MInst) * m->count, cudaMemcpyHostToDevice, m->st));
+  MCU(cudaGraphLaunch(m->graph2, m->st));
   MCU(cudaEventRecord(m->ev[1], m->st));
   const size_t rec = (size_t)m->count * (m->n_eval + 1);
   MCU(cudaMemcpyAsync(order, m->d_r, sizeof(float) * rec, cudaMemcpyDeviceToHost, m->st));

@@ -3,7 +3,8 @@
 // accumulated in FP32 in tensor memory.  One CTA computes a 128-row tile times all
 // NCOL columns (NCOL <= 512, the whole TMEM), looping over row tiles (persistent).
 //
-// Roles (160 threads): warp 0 lane 0 streams A and X tiles with TMA into a ring of
+// Roles (160 threads): warp 0 lane 0 streams A and X tiles with TMA (64-byte swizzle, 32
+// BF16 of K per stage, so that even NCOL = 512 keeps 5 stages in flight) into a ring of
 // STAGES shared-memory stages; warp 1 lane 0 issues the MMAs (M = 128, N = min(NCOL,
 // 256), K = 16 per instruction) and commits each stage back to the producer; warps 1-4
 // read the accumulator (warp w owns TMEM lanes 32*(w%4)..+31, one tile row per thread)
@@ -15,7 +16,8 @@
 namespace kura {
 
 constexpr int TG_BM = 128;  // rows per tile (M of one MMA)
-constexpr int TG_BK = 64;   // K per stage (one 128-byte swizzle row of BF16)
+constexpr int TG_BK = 32;   // K per stage (one 64-byte swizzle row of BF16)
+constexpr int TG_ROWB = TG_BK * 2;  // bytes per tile row
 constexpr int TG_THREADS = 160;
 
 template <int NCOL> struct TGCfg {
@@ -24,7 +26,7 @@ template <int NCOL> struct TGCfg {
   static constexpr int A_BYTES = TG_BM * TG_BK * 2;
   static constexpr int X_BYTES = NCOL * TG_BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + X_BYTES;
-  static constexpr int STAGES = (200 * 1024) / STAGE_BYTES > 6 ? 6 : (200 * 1024) / STAGE_BYTES;
+  static constexpr int STAGES = (200 * 1024) / STAGE_BYTES > 8 ? 8 : (200 * 1024) / STAGE_BYTES;
   static constexpr int TMEM_COLS = NCOL < 32 ? 32 : NCOL;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
   static_assert(NCOL % 16 == 0 && NCOL <= 512, "NCOL");
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
           for (int h = 0; h < (NCOL + 255) / 256; ++h) {
             const int rows = NCOL - h * 256 < 256 ? NCOL - h * 256 : 256;
             (void)rows;
-            umma::tma_load_2d(st + C::A_BYTES + h * 256 * 128, &tmX, &full[s], kt * TG_BK, h * 256);
+            umma::tma_load_2d(st + C::A_BYTES + h * 256 * TG_ROWB, &tmX, &full[s], kt * TG_BK, h * 256);
           }
           ++issued;
           if (++s == C::STAGES) { s = 0; ph ^= 1; }
@@ -127,10 +129,10 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
             const uint32_t x0 = a0 + C::A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < TG_BK / 16; ++kk) {
-              const uint64_t ad = umma::sw128_desc(a0 + kk * 32);
+              const uint64_t ad = umma::sw64_desc(a0 + kk * 32);
 #pragma unroll
               for (int h = 0; h < C::NH; ++h) {
-                const uint64_t xd = umma::sw128_desc(x0 + h * C::NMMA * 128 + kk * 32);
+                const uint64_t xd = umma::sw64_desc(x0 + h * C::NMMA * TG_ROWB + kk * 32);
                 umma::mma_bf16(tmem + h * C::NMMA, ad, xd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
               }
             }
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
 }
 
 // host: 2-D tensor map of a K-major BF16 matrix [rows][k] (row stride k elements) with a
-// (64 x box_rows) box and the 128-byte swizzle.  cuTensorMapEncodeTiled is fetched from
+// (TG_BK x box_rows) box and the 64-byte swizzle.  cuTensorMapEncodeTiled is fetched from
 // the driver at run time, so the library does not link libcuda.
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -185,7 +187,7 @@ inline int make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t k, uint64
   cuuint32_t box[2] = {(cuuint32_t)TG_BK, box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : -2;
 }

@@ -2,8 +2,9 @@
 // TMA tile loads, mbarriers with bounded waits, TMEM allocation, BF16 MMA with FP32
 // accumulation in TMEM, and TMEM loads.  Written as inline PTX (no CUTLASS).
 //
-// Shared-memory operand tiles are K-major with the 128-byte swizzle that TMA writes
-// (CU_TENSOR_MAP_SWIZZLE_128B): rows of 64 BF16 (128 B), 8-row atoms of 1024 B.
+// Shared-memory operand tiles are K-major with the swizzle that TMA writes: the 128-byte
+// swizzle (rows of 64 BF16, 8-row atoms of 1024 B) or the 64-byte one (rows of 32 BF16,
+// 8-row atoms of 512 B).
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -97,6 +98,16 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   d |= (uint64_t)((1024u >> 4) & 0x3FFFu) << 32;  // stride byte offset: 8 rows x 128 B
   d |= (uint64_t)1 << 46;                    // descriptor version
   d |= (uint64_t)2 << 61;                    // swizzle: 128 B
+  return d;
+}
+// The same for the 64-byte swizzle (swizzle mode 4 = 64 B): 8-row atoms of 512 B.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)(1u) << 16;                     // leading byte offset (unused), 16 B
+  d |= (uint64_t)((512u >> 4) & 0x3FFFu) << 32;  // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                        // descriptor version
+  d |= (uint64_t)4 << 61;                        // swizzle: 64 B
   return d;
 }
 // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9 and
