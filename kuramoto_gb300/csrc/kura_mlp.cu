@@ -48,7 +48,7 @@ template <int NCOL> struct FwdEpi {
   bf16* HT;  // [NCOL][Bt]
   float* S;  // [Bt][NCOL]
   float* Y;  // [Bt][NCOL]
-  __device__ void row(uint32_t taddr, int row, int m0) {
+  __device__ void row(uint32_t taddr, int row, int m0, int) {
     const int r = m0 + row;
 #pragma unroll 1
     for (int c0 = 0; c0 < NCOL; c0 += 16) {
@@ -88,7 +88,7 @@ template <int NCOL> struct FwdEpi {
 template <int NCOL> struct DwEpi {
   float* G;  // [out_p][NCOL]
   int out_p;
-  __device__ void row(uint32_t taddr, int row, int m0) {
+  __device__ void row(uint32_t taddr, int row, int m0, int) {
     const int r = m0 + row;
 #pragma unroll 1
     for (int c0 = 0; c0 < NCOL; c0 += 16) {
@@ -109,7 +109,7 @@ template <int NCOL> struct DhEpi {
   bf16* dZ;        // [Bt][NCOL]
   bf16* dZT;       // [NCOL][Bt]
   int Bt;
-  __device__ void row(uint32_t taddr, int row, int m0) {
+  __device__ void row(uint32_t taddr, int row, int m0, int) {
     const int r = m0 + row;
 #pragma unroll 1
     for (int c0 = 0; c0 < NCOL; c0 += 16) {
@@ -305,7 +305,7 @@ constexpr unsigned long long GEMM_LIMIT_NS = 20000000000ull;
 template <int NCOL, class Epi>
 cudaError_t gemm(kura_mlp* m, const CUtensorMap& a, const CUtensorMap& x, int mtiles, int ktiles, const Epi& e) {
   kura::k_tensor_gemm<NCOL, Epi><<<std::min(mtiles, m->sms), kura::TG_THREADS, kura::TGCfg<NCOL>::SMEM, m->st>>>(
-      a, x, mtiles, ktiles, e, m->err, GEMM_LIMIT_NS, nullptr);
+      a, x, mtiles, ktiles, 1, 0, e, m->err, GEMM_LIMIT_NS, nullptr);
   return cudaGetLastError();
 }
 

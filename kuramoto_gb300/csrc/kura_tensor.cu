@@ -58,6 +58,14 @@ struct TView {
   float* Flo;  // [2][bp][np] partial couplings of the A_lo pass (general adjacency)
 };
 
+// row of X holding column q (0 hi cos, 1 hi sin, 2 lo cos, 3 lo sin) of trajectory b: the
+// trajectories are grouped by 64 so that each group's 4 x 64 columns are one contiguous
+// block, the column block of one GEMM work unit
+__host__ __device__ __forceinline__ int x_bph(int bp) { return bp > 64 ? 64 : bp; }
+__device__ __forceinline__ size_t xrow(int q, int b, int bp) {
+  const int g = x_bph(bp);
+  return (size_t)(b / g) * 4 * g + (size_t)q * g + (b % g);
+}
 __device__ __forceinline__ int slot_k1(int rot_g) { return rot_g ? 6 : 0; }
 __device__ __forceinline__ int slot_k7(int rot_g) { return rot_g ? 0 : 6; }
 
@@ -177,10 +185,10 @@ __global__ void k_t_stage(TView v, const TCoef* src) {
   const __nv_bfloat16 ch = __float2bfloat16_rn(cs), sh = __float2bfloat16_rn(sn);
   const __nv_bfloat16 cl = __float2bfloat16_rn(cs - __bfloat162float(ch));
   const __nv_bfloat16 sl = __float2bfloat16_rn(sn - __bfloat162float(sh));
-  v.X[((size_t)0 * v.bp + b) * v.np + i] = ch;
-  v.X[((size_t)1 * v.bp + b) * v.np + i] = sh;
-  v.X[((size_t)2 * v.bp + b) * v.np + i] = cl;
-  v.X[((size_t)3 * v.bp + b) * v.np + i] = sl;
+  v.X[xrow(0, b, v.bp) * v.np + i] = ch;
+  v.X[xrow(1, b, v.bp) * v.np + i] = sh;
+  v.X[xrow(2, b, v.bp) * v.np + i] = cl;
+  v.X[xrow(3, b, v.bp) * v.np + i] = sl;
   if (s.store_y7 || s.rec) {
     f2 y = two_sum(s2.hi, lo);
     long long w = v.ph_w[boff + i];
@@ -199,13 +207,14 @@ __global__ void k_t_stage(TView v, const TCoef* src) {
 }
 
 // ---------------------------------------------------------------- GEMM epilogues
-// accumulator columns: [hi cos | hi sin | lo cos | lo sin], bp columns each
+// accumulator columns of work unit sp: [hi cos | hi sin | lo cos | lo sin] of trajectories
+// sp*BP .. sp*BP + BP - 1, BP columns each
 template <int BP> struct KuraEpi {
   TView v;
   const TCoef* src;
   float invn;
   int has_lo;
-  __device__ void row(uint32_t taddr, int row, int m0) {
+  __device__ void row(uint32_t taddr, int row, int m0, int sp) {
     const int i = m0 + row;
 #pragma unroll 1
     for (int b0 = 0; b0 < BP; b0 += 16) {
@@ -218,7 +227,7 @@ template <int BP> struct KuraEpi {
       if (i >= v.n) continue;
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        const int b = b0 + j;
+        const int b = sp * BP + b0 + j;
         if (b >= v.B) break;
         const TCoef& s = src[b];
         if (!s.active) continue;
@@ -245,7 +254,7 @@ template <int BP> struct KuraEpi {
 template <int BP> struct LoEpi {
   TView v;
   const TCoef* src;
-  __device__ void row(uint32_t taddr, int row, int m0) {
+  __device__ void row(uint32_t taddr, int row, int m0, int sp) {
     const int i = m0 + row;
 #pragma unroll 1
     for (int b0 = 0; b0 < BP; b0 += 16) {
@@ -256,7 +265,7 @@ template <int BP> struct LoEpi {
       if (i >= v.n) continue;
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        const int b = b0 + j;
+        const int b = sp * BP + b0 + j;
         if (b >= v.B) break;
         v.Flo[((size_t)0 * v.bp + b) * v.np + i] = hc[j];
         v.Flo[((size_t)1 * v.bp + b) * v.np + i] = hs[j];
@@ -573,8 +582,10 @@ int TensorEngine::init(int64_t n, int k, int batch, int seed, double atol, doubl
   TCU(cudaHostAlloc((void**)&I.h_done, sizeof(int), cudaHostAllocDefault));
   TCU(cudaEventCreate(&I.ev0));
   TCU(cudaEventCreate(&I.ev1));
-  if (make_tmap_bf16(&I.tmA, I.Ahi, np, np, TG_BM) || make_tmap_bf16(&I.tmX, I.X, np, 4 * bp, std::min<int>(256, 4 * I.bp)) ||
-      make_tmap_bf16(&I.tmXhi, I.X, np, 2 * bp, std::min<int>(256, 2 * I.bp))) {
+  // X is [4 bp][np]: a work unit's column block is 4 * x_bph(bp) rows (its hi + lo columns),
+  // of which the A_lo pass reads the first half
+  if (make_tmap_bf16(&I.tmA, I.Ahi, np, np, TG_BM) || make_tmap_bf16(&I.tmX, I.X, np, 4 * bp, 4 * x_bph(I.bp)) ||
+      make_tmap_bf16(&I.tmXhi, I.X, np, 4 * bp, 2 * x_bph(I.bp))) {
     g_terr = "cuTensorMapEncodeTiled failed";
     return KURA_ERR_CUDA;
   }
@@ -689,33 +700,37 @@ template <int NCOL>
 static cudaError_t launch_gemm(TensorEngine::Impl& I, const TCoef* src, int mode, const int* run_flag) {
   TView v{I.n, I.np, I.bp, I.B, mode, I.omega, I.ph_hi, I.ph_lo, I.ph_w, I.g, I.X, I.x32, I.fin_theta, I.fin_coup,
           I.Flo};
-  constexpr int BP = NCOL / 4;
+  constexpr int BP = NCOL / 4;  // trajectories per work unit
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, I.device);
   const int mtiles = I.np / TG_BM, ktiles = I.np / TG_BK;
-  const int grid = std::min(mtiles, sms);
+  const int nsplit = I.bp / BP, xstride = 4 * BP;
+  const int grid = std::min(mtiles * nsplit, sms);
   const unsigned long long limit = 20000000000ull;
   if (I.has_lo) {
     auto kl = k_tensor_gemm<NCOL / 2, LoEpi<BP>>;
     cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL / 2>::SMEM);
     LoEpi<BP> le{v, src};
-    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, ktiles, le, I.err, limit, run_flag);
+    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, ktiles, nsplit, xstride, le,
+                                                             I.err, limit, run_flag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   auto k = k_tensor_gemm<NCOL, KuraEpi<BP>>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL>::SMEM);
   KuraEpi<BP> ep{v, src, 1.0f / (float)I.n, I.has_lo ? 1 : 0};
-  k<<<grid, TG_THREADS, TGCfg<NCOL>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, ktiles, ep, I.err, limit, run_flag);
+  k<<<grid, TG_THREADS, TGCfg<NCOL>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, ktiles, nsplit, xstride, ep, I.err, limit,
+                                                   run_flag);
   return cudaGetLastError();
 }
 
+// one unit holds up to 64 trajectories (NCOL = 256: two accumulators fit in TMEM); a batch
+// of 128 is two column blocks per row tile
 static cudaError_t gemm(TensorEngine::Impl& I, const TCoef* src, int mode, const int* run_flag) {
   switch (I.bp) {
     case 16: return launch_gemm<64>(I, src, mode, run_flag);
     case 32: return launch_gemm<128>(I, src, mode, run_flag);
-    case 64: return launch_gemm<256>(I, src, mode, run_flag);
-    default: return launch_gemm<512>(I, src, mode, run_flag);
+    default: return launch_gemm<256>(I, src, mode, run_flag);
   }
 }
 

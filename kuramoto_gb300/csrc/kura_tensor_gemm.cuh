@@ -1,14 +1,15 @@
 // kura_tensor_gemm.cuh -- tcgen05 GEMM with a fused epilogue:
 //   C[m][c] = sum_k A[m][k] * X[c][k]      (A: M x K BF16, X: NCOL x K BF16, both K-major)
-// accumulated in FP32 in tensor memory.  One CTA computes a 128-row tile times all
-// NCOL columns (NCOL <= 512, the whole TMEM), looping over row tiles (persistent).
+// accumulated in FP32 in tensor memory.  A work unit is a 128-row tile times one block of
+// NCOL columns (NCOL <= 512); CTAs loop over units (persistent).
 //
-// Roles (160 threads): warp 0 lane 0 streams A and X tiles with TMA (64-byte swizzle, 32
+// Roles (192 threads): warp 0 lane 0 streams A and X tiles with TMA (64-byte swizzle, 32
 // BF16 of K per stage, so that even NCOL = 512 keeps 5 stages in flight) into a ring of
 // STAGES shared-memory stages; warp 1 lane 0 issues the MMAs (M = 128, N = min(NCOL,
-// 256), K = 16 per instruction) and commits each stage back to the producer; warps 1-4
+// 256), K = 16 per instruction) and commits each stage back to the producer; warps 2-5
 // read the accumulator (warp w owns TMEM lanes 32*(w%4)..+31, one tile row per thread)
-// and call the epilogue.  Every wait is bounded: on a timeout the CTA records an error,
+// and call the epilogue.  With NCOL <= 256 two accumulators alternate in TMEM, so the MMAs
+// of one unit run while the epilogue reads the previous one.  Every wait is bounded: on a timeout the CTA records an error,
 // stops issuing work, waits (bounded) for its own TMA copies, frees TMEM and returns.
 #pragma once
 #include "kura_umma.cuh"
@@ -18,7 +19,7 @@ namespace kura {
 constexpr int TG_BM = 128;  // rows per tile (M of one MMA)
 constexpr int TG_BK = 32;   // K per stage (one 64-byte swizzle row of BF16)
 constexpr int TG_ROWB = TG_BK * 2;  // bytes per tile row
-constexpr int TG_THREADS = 160;
+constexpr int TG_THREADS = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 
 template <int NCOL> struct TGCfg {
   static constexpr int NMMA = NCOL > 256 ? 256 : NCOL;  // N of one MMA instruction
@@ -27,29 +28,36 @@ template <int NCOL> struct TGCfg {
   static constexpr int X_BYTES = NCOL * TG_BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + X_BYTES;
   static constexpr int STAGES = (200 * 1024) / STAGE_BYTES > 8 ? 8 : (200 * 1024) / STAGE_BYTES;
-  static constexpr int TMEM_COLS = NCOL < 32 ? 32 : NCOL;
+  static constexpr int ACC_COLS = NCOL < 32 ? 32 : NCOL;          // one accumulator
+  static constexpr int NACC = 2 * ACC_COLS <= 512 ? 2 : 1;          // double-buffered when TMEM allows
+  static constexpr int TMEM_COLS = ACC_COLS * NACC;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
   static_assert(NCOL % 16 == 0 && NCOL <= 512, "NCOL");
   static_assert(STAGES >= 2, "stages");
 };
 
-// Epilogue interface: Epi::row(taddr, row, m0) is called by every thread of warps 1-4
-// with taddr = TMEM address of this thread's accumulator row (lane field set, column 0).
+// Work units: (128-row tile, column block); column block sp covers X rows
+// sp * xstride .. + NCOL.  Epilogue interface: Epi::row(taddr, row, m0, sp) is called by
+// every thread of warps 1-4 with taddr = TMEM address of this thread's accumulator row
+// (lane field set, column 0).  With NCOL <= 256 the accumulator is double-buffered in TMEM,
+// so one unit's epilogue overlaps the next unit's MMAs.
 template <int NCOL, class Epi>
 __global__ void __launch_bounds__(TG_THREADS, 1)
     k_tensor_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int mtiles,
-                  int ktiles, Epi epi, int* err, unsigned long long limit_ns, const int* run_flag) {
+                  int ktiles, int nsplit, int xstride, Epi epi, int* err, unsigned long long limit_ns,
+                  const int* run_flag) {
   using C = TGCfg<NCOL>;
   if (run_flag && *run_flag == 0) return;  // nothing to compute (every column inactive)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = (uint64_t*)(smem + C::STAGES * C::STAGE_BYTES);
-  uint64_t* full = bars;                    // [STAGES]
-  uint64_t* empty = bars + C::STAGES;       // [STAGES]
-  uint64_t* accfull = bars + 2 * C::STAGES; // MMAs of a tile done
-  uint64_t* accempty = accfull + 1;         // epilogue of a tile done (4 warp arrivals)
-  uint32_t* tmem_slot = (uint32_t*)(accempty + 1);
+  uint64_t* full = bars;                     // [STAGES]
+  uint64_t* empty = bars + C::STAGES;        // [STAGES]
+  uint64_t* accfull = bars + 2 * C::STAGES;  // [2] MMAs of a unit done
+  uint64_t* accempty = accfull + 2;          // [2] epilogue of a unit done (4 warp arrivals)
+  uint32_t* tmem_slot = (uint32_t*)(accempty + 2);
   volatile int* sabort = (volatile int*)(tmem_slot + 1);
+  const int units = mtiles * nsplit;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -57,14 +65,16 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
       umma::mbar_init(&full[s], 1);
       umma::mbar_init(&empty[s], 1);
     }
-    umma::mbar_init(accfull, 1);
-    umma::mbar_init(accempty, 4);
+    for (int q = 0; q < 2; ++q) {
+      umma::mbar_init(&accfull[q], 1);
+      umma::mbar_init(&accempty[q], 4);
+    }
     *sabort = 0;
     umma::fence_barrier_init();
     umma::prefetch_tmap(&tmA);
     umma::prefetch_tmap(&tmX);
   }
-  if (warp == 2) umma::tmem_alloc(tmem_slot, C::TMEM_COLS);
+  if (warp == 2) umma::tmem_alloc(tmem_slot, C::TMEM_COLS);  // warp 2 also frees it
   umma::tc_fence_before();
   __syncthreads();
   umma::tc_fence_after();
@@ -76,9 +86,9 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
     if (lane == 0) {
       int s = 0;
       uint32_t ph = 0;
-      long long issued = 0, consumed_hint = 0;
-      (void)consumed_hint;
-      for (int tile = blockIdx.x; tile < mtiles && !*sabort; tile += gridDim.x) {
+      long long issued = 0;
+      for (int u = blockIdx.x; u < units && !*sabort; u += gridDim.x) {
+        const int tile = u / nsplit, xr0 = (u % nsplit) * xstride;
         for (int kt = 0; kt < ktiles; ++kt) {
           if (!umma::mbar_wait(&empty[s], ph ^ 1, limit_ns, sabort)) {
             *sabort = 1;
@@ -88,11 +98,8 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
           umma::mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
           umma::tma_load_2d(st, &tmA, &full[s], kt * TG_BK, tile * TG_BM);
 #pragma unroll
-          for (int h = 0; h < (NCOL + 255) / 256; ++h) {
-            const int rows = NCOL - h * 256 < 256 ? NCOL - h * 256 : 256;
-            (void)rows;
-            umma::tma_load_2d(st + C::A_BYTES + h * 256 * TG_ROWB, &tmX, &full[s], kt * TG_BK, h * 256);
-          }
+          for (int h = 0; h < (NCOL + 255) / 256; ++h)
+            umma::tma_load_2d(st + C::A_BYTES + h * 256 * TG_ROWB, &tmX, &full[s], kt * TG_BK, xr0 + h * 256);
           ++issued;
           if (++s == C::STAGES) { s = 0; ph ^= 1; }
         }
@@ -107,44 +114,51 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
         umma::mbar_wait(&full[ds], dph, limit_ns, nullptr);
       }
     }
-  } else {
-    // ---------------- MMA issue (warp 1 lane 0) and epilogue (warps 1-4)
-    int s = 0;
-    uint32_t ph = 0;
-    uint32_t it = 0;
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
-    for (int tile = blockIdx.x; tile < mtiles; tile += gridDim.x, ++it) {
-      if (warp == 1) {
-        if (lane == 0 && !*sabort) {
-          // the accumulator must have been read out by the previous tile's epilogue
-          if (!umma::mbar_wait(accempty, (it & 1) ^ 1, limit_ns, sabort)) *sabort = 1;
-          umma::tc_fence_after();
-          for (int kt = 0; kt < ktiles && !*sabort; ++kt) {
-            if (!umma::mbar_wait(&full[s], ph, limit_ns, sabort)) {
-              *sabort = 1;
-              break;
-            }
-            umma::tc_fence_after();
-            const uint32_t a0 = umma::smem_u32(smem + s * C::STAGE_BYTES);
-            const uint32_t x0 = a0 + C::A_BYTES;
-#pragma unroll
-            for (int kk = 0; kk < TG_BK / 16; ++kk) {
-              const uint64_t ad = umma::sw64_desc(a0 + kk * 32);
-#pragma unroll
-              for (int h = 0; h < C::NH; ++h) {
-                const uint64_t xd = umma::sw64_desc(x0 + h * C::NMMA * TG_ROWB + kk * 32);
-                umma::mma_bf16(tmem + h * C::NMMA, ad, xd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
-              }
-            }
-            umma::mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
-            if (++s == C::STAGES) { s = 0; ph ^= 1; }
-          }
-          umma::mma_commit(accfull);
+  } else if (warp == 1) {
+    // ---------------- MMA issue (lane 0): runs ahead of the epilogue by one accumulator
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      uint32_t it = 0;
+      for (int u = blockIdx.x; u < units && !*sabort; u += gridDim.x, ++it) {
+        const uint32_t buf = it % C::NACC, use = it / C::NACC;  // accumulator and its use count
+        const uint32_t tacc = tmem + buf * C::ACC_COLS;
+        // the accumulator must have been read out by the epilogue of its previous use
+        if (!umma::mbar_wait(&accempty[buf], (use & 1) ^ 1, limit_ns, sabort)) {
+          *sabort = 1;
+          break;
         }
-        __syncwarp();
+        umma::tc_fence_after();
+        for (int kt = 0; kt < ktiles && !*sabort; ++kt) {
+          if (!umma::mbar_wait(&full[s], ph, limit_ns, sabort)) {
+            *sabort = 1;
+            break;
+          }
+          umma::tc_fence_after();
+          const uint32_t a0 = umma::smem_u32(smem + s * C::STAGE_BYTES);
+          const uint32_t x0 = a0 + C::A_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < TG_BK / 16; ++kk) {
+            const uint64_t ad = umma::sw64_desc(a0 + kk * 32);
+#pragma unroll
+            for (int h = 0; h < C::NH; ++h) {
+              const uint64_t xd = umma::sw64_desc(x0 + h * C::NMMA * TG_ROWB + kk * 32);
+              umma::mma_bf16(tacc + h * C::NMMA, ad, xd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+            }
+          }
+          umma::mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+          if (++s == C::STAGES) { s = 0; ph ^= 1; }
+        }
+        umma::mma_commit(&accfull[buf]);
       }
-      // epilogue
-      bool ok = umma::mbar_wait(accfull, it & 1, limit_ns, sabort);
+    }
+  } else {
+    // ---------------- epilogue (warps 2-5; warp w reads TMEM lanes 32*(w%4)..+31)
+    const int q = warp & 3;
+    uint32_t it = 0;
+    for (int u = blockIdx.x; u < units; u += gridDim.x, ++it) {
+      const uint32_t buf = it % C::NACC, use = it / C::NACC;
+      bool ok = umma::mbar_wait(&accfull[buf], use & 1, limit_ns, sabort);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) {
         if (lane == 0) *sabort = 1;
@@ -152,10 +166,10 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
       }
       umma::tc_fence_after();
       const int row = q * 32 + lane;
-      epi.row(tmem + ((uint32_t)(q * 32) << 16), row, tile * TG_BM);
+      epi.row(tmem + buf * C::ACC_COLS + ((uint32_t)(q * 32) << 16), row, (u / nsplit) * TG_BM, u % nsplit);
       umma::tc_fence_before();
       __syncwarp();
-      if (lane == 0) umma::mbar_arrive(accempty);
+      if (lane == 0) umma::mbar_arrive(&accempty[buf]);
     }
   }
   __syncthreads();
