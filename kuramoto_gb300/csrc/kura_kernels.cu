@@ -334,6 +334,132 @@ struct Engine {
   }
 
   // ---- one coupling evaluation for every active trajectory (one grid barrier)
+  // Phase A of the regenerated coupling when every warp serves every trajectory and the
+  // (cos, sin) of the CTA's rows live in shared memory.  Pass 1 takes the thread's
+  // (row, trajectory) pairs four at a time, all loads of a batch before its arithmetic, so the
+  // L2 latencies of different trajectories overlap (a thread has only 2-3 rows per
+  // trajectory); it writes (cos, sin) to shared memory.  Pass 2 forms each trajectory's
+  // projections and r sums from shared memory (the thread reads back its own rows).
+  __device__ void phase_a_pairs(bool want_r, int npw) {
+    const int ld = p.ld, k = p.k;
+    const int nrow = tid < r1 - r0 ? (r1 - r0 - tid + KT - 1) / KT : 0;
+    const int npairs = nrow * B;
+    const bool emit_mode = (p.dense_level >= 1 && p.mode == MODE_INTEGRATE) || p.mode == MODE_FINAL;
+    constexpr int U = 4;
+    for (int p0 = 0; p0 < npairs; p0 += U) {
+      float om[U], yh[U], yl[U], gs[U];
+      int bq[U], iq[U];
+      bool act[U];
+#pragma unroll
+      for (int q = 0; q < U; ++q) {
+        const int pi = p0 + q;
+        const int b = pi < npairs ? pi / nrow : 0;
+        const int i = r0 + tid + (pi < npairs ? pi - b * nrow : 0) * KT;
+        const SrcB& s = sb[b];
+        act[q] = pi < npairs && s.active;
+        bq[q] = b;
+        iq[q] = i;
+        om[q] = yh[q] = yl[q] = gs[q] = 0.f;
+        if (act[q]) {
+          const size_t boff = ((size_t)s.base * B + b) * ld;
+          om[q] = p.omega[i];
+          yh[q] = p.ph_hi[boff + i];
+          yl[q] = p.ph_lo[boff + i];
+          const int nW = s.nW;
+#pragma unroll
+          for (int j = 0; j < 7; ++j)
+            if (j < nW) gs[q] = __fmaf_rn(s.W[j], p.g[((size_t)s.slot[j] * B + b) * ld + i], gs[q]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < U; ++q) {
+        if (!act[q]) continue;
+        const int b = bq[q], i = iq[q];
+        const SrcB& s = sb[b];
+        const f2 pr = two_prod(om[q], s.m_hi);
+        const f2 s1 = two_sum(yh[q], pr.hi);
+        const f2 s2 = two_sum(s1.hi, gs[q]);
+        const float lo = yl[q] + ((s1.lo + s2.lo) + __fmaf_rn(om[q], s.m_lo, pr.lo));
+        float sn, cs;
+        sincos_pair(s2.hi, lo, &sn, &cs);
+        xrow(b)[i] = make_float2(cs, sn);
+        const bool emit = s.rec && emit_mode;
+        if (s.store_y7 || emit) {
+          const size_t boff = ((size_t)s.base * B + b) * ld;
+          f2 y = two_sum(s2.hi, lo);
+          long long w = p.ph_w[boff + i];
+          if (s.store_y7) {
+            float hi7 = y.hi, lo7 = y.lo;
+            long long w7 = w;
+            wrap_phase(hi7, lo7, w7);
+            size_t o = ((size_t)(s.base ^ 1) * B + b) * ld + i;
+            p.ph_hi[o] = hi7;
+            p.ph_lo[o] = lo7;
+            p.ph_w[o] = w7;
+          } else {
+            double th = (double)w * TWO_PI_D + (double)y.hi + (double)y.lo;
+            if (p.mode == MODE_INTEGRATE)
+              p.out_theta[((size_t)b * p.ring + s.oslot) * ld + i] = (float)th;
+            else
+              p.fin_theta[(size_t)b * ld + i] = (float)th;
+          }
+        }
+      }
+    }
+    for (int b = 0; b < B; ++b) {
+      float acc[PW];
+#pragma unroll
+      for (int v = 0; v < PW; ++v) acc[v] = 0.f;
+      if (sb[b].active) {
+        const float2* xb = xrow(b);
+        // sum_n u_mn x_n = 2 (sum over the n with u_mn = +1) - sum_n x_n: one predicated add
+        // per mode and row (the factor bits above k are zero)
+        float sx = 0.f, sy = 0.f;
+        for (int i = r0 + tid; i < r1; i += KT) {
+          const float2 x = xb[i];
+          const uint32_t u = ubits[i - r0];
+          sx += x.x;
+          sy += x.y;
+#pragma unroll
+          for (int m = 0; m < KMAX; ++m) {
+            if (u & (1u << m)) {
+              acc[2 * m] += x.x;
+              acc[2 * m + 1] += x.y;
+            }
+          }
+        }
+#pragma unroll
+        for (int m = 0; m < KMAX; ++m) {
+          acc[2 * m] = 2.f * acc[2 * m] - sx;
+          acc[2 * m + 1] = 2.f * acc[2 * m + 1] - sy;
+        }
+        if (want_r) {
+          acc[PW - 2] = sx;
+          acc[PW - 1] = sy;
+        }
+      }
+      // compact layout: [2k projections][sum cos, sum sin]
+      float* dst = red + (warp * BMAX + b) * PW;
+#pragma unroll
+      for (int c0 = 0; c0 < 2 * KMAX; c0 += 16) {
+        float v16[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v16[j] = acc[c0 + j];
+        warp_reduce_scatter16(v16, lane);
+        const int v = c0 + scatter16_index(lane);
+        if (!(lane & 1) && v < 2 * k) dst[v] = v16[0];
+      }
+      if (want_r) {
+        float t0 = warp_sum(acc[PW - 2]);
+        float t1 = warp_sum(acc[PW - 1]);
+        if (lane == 0) {
+          dst[npw - 2] = t0;
+          dst[npw - 1] = t1;
+        }
+      }
+    }
+  }
+
   __device__ bool coupling_eval(bool want_r) {
     const int n = p.n, ld = p.ld, k = p.k;
     const bool need_part = (COUP == KURA_COUPLING_VOLCANO) || want_r;
@@ -342,6 +468,9 @@ struct Engine {
     // own group of KW/B warps, so the trajectories of a batch proceed side by side.
     int b0, b1, lt, gt;
     work_map(b0, b1, lt, gt);
+    if (COUP == KURA_COUPLING_VOLCANO && xs != nullptr && all_warps_mode())
+      phase_a_pairs(want_r, npw);
+    else
     for (int b = b0; b < b1; ++b) {
       const SrcB& s = sb[b];
       float acc[PW];
@@ -414,23 +543,28 @@ struct Engine {
             }
           }
           if (COUP == KURA_COUPLING_VOLCANO) {
-            // u_m = -1 flips the sign bit: sum_n u_mn (cos_n, sin_n)
-            const uint32_t nu = ~ub[q];
-            const uint32_t cb = __float_as_uint(cs), sbits = __float_as_uint(sn);
+            // sums over the rows with u_mn = +1 (the factor bits above k are zero)
 #pragma unroll
             for (int m = 0; m < KMAX; ++m) {
-              if (m < k) {
-                const uint32_t sg = (nu << (31 - m)) & 0x80000000u;
-                acc[2 * m] += __uint_as_float(cb ^ sg);
-                acc[2 * m + 1] += __uint_as_float(sbits ^ sg);
+              if (ub[q] & (1u << m)) {
+                acc[2 * m] += cs;
+                acc[2 * m + 1] += sn;
               }
             }
           }
-          if (want_r) {
+          if (COUP == KURA_COUPLING_VOLCANO || want_r) {
             acc[PW - 2] += cs;
             acc[PW - 1] += sn;
           }
           }
+        }
+      }
+      if (COUP == KURA_COUPLING_VOLCANO) {
+        // sum_n u_mn x_n = 2 (sum over u_mn = +1) - sum_n x_n
+#pragma unroll
+        for (int m = 0; m < KMAX; ++m) {
+          acc[2 * m] = 2.f * acc[2 * m] - acc[PW - 2];
+          acc[2 * m + 1] = 2.f * acc[2 * m + 1] - acc[PW - 1];
         }
       }
       if (need_part) {

@@ -215,21 +215,25 @@ struct Multi {
         p.ph_w[(base ^ 1) * T + gi] = w7;
       }
       if (proj) {
-        // u_m = -1 flips the sign bit: sum_n u_mn (cos_n, sin_n)
-        const uint32_t nu = ~(uint32_t)ubits[i - r0];
-        const uint32_t cb = __float_as_uint(cs), sb = __float_as_uint(sn);
+        // sum over the rows with u_mn = +1 (the factor bits above k are zero)
+        const uint32_t u = ubits[i - r0];
 #pragma unroll
         for (int m = 0; m < M_KMAX; ++m) {
-          if (m < k) {  // uniform over the cluster: the rank of the network
-            const uint32_t sg = (nu << (31 - m)) & 0x80000000u;
-            acc[2 * m] += __uint_as_float(cb ^ sg);
-            acc[2 * m + 1] += __uint_as_float(sb ^ sg);
+          if (u & (1u << m)) {
+            acc[2 * m] += cs;
+            acc[2 * m + 1] += sn;
           }
         }
       }
-      if (want_r) {
-        acc[M_RX] += cs;
-        acc[M_RX + 1] += sn;
+      acc[M_RX] += cs;
+      acc[M_RX + 1] += sn;
+    }
+    // sum_n u_mn x_n = 2 (sum over u_mn = +1) - sum_n x_n
+    if (proj) {
+#pragma unroll
+      for (int m = 0; m < M_KMAX; ++m) {
+        acc[2 * m] = 2.f * acc[2 * m] - acc[M_RX];
+        acc[2 * m + 1] = 2.f * acc[2 * m + 1] - acc[M_RX + 1];
       }
     }
     if (proj || want_r) cluster_reduce(acc, proj ? 2 * k : 0, want_r);
