@@ -106,7 +106,7 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[1] = o; o += align16(7 * bmax * (int)sizeof(SrcB));  // [0]: current source; [1..6]: stages 2..7
   off[2] = o; o += align16(KW * bmax * pw * 4);          // red
   off[3] = o; o += align16(bmax * pw * 4);               // rsum
-  int sl = KT > bmax * pw ? KT : bmax * pw;
+  int sl = 2 * KT > bmax * pw ? 2 * KT : bmax * pw;
   off[4] = o; o += align16(sl * 4);                      // slice
   off[5] = o; o += align16(16 * 4);                      // flags
   off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
@@ -282,11 +282,13 @@ struct Engine {
   __device__ void gather_partials(int npw) {
     const int par = (nbar - 1) & 1;  // the parity published before the barrier just passed
     const int NV = B * npw;
-    // the slicing does not depend on the batch size, so a trajectory's sums (and so its
-    // whole integration) are the same bits whether it runs alone or inside a batch
-    int S = KT / (8 * npw);
+    // slices of at most 16 CTAs where the slice buffer (2 KT values for up to 8
+    // trajectories) allows, so that every thread needs one round of loads; the slicing does
+    // not depend on the batch size, so a trajectory's sums (and so its whole integration)
+    // are the same bits whether it runs alone or inside a batch
+    int S = 2 * KT / (8 * npw);
     if (S < 1) S = 1;
-    if (S > G) S = G;
+    if (S > (G + 15) / 16) S = (G + 15) / 16;
     const size_t stride = (size_t)B * PW_MAX;
     for (int t = tid; t < S * NV; t += KT) {
       int v = t % NV, sl = t / NV;
@@ -346,19 +348,28 @@ struct Engine {
     const int npairs = nrow * B;
     const bool emit_mode = (p.dense_level >= 1 && p.mode == MODE_INTEGRATE) || p.mode == MODE_FINAL;
     constexpr int U = 4;
+    int bc = 0, jc = 0;  // (trajectory, row) of the next pair: pair p = b * nrow + j
     for (int p0 = 0; p0 < npairs; p0 += U) {
-      float om[U], yh[U], yl[U], gs[U];
+      float om[U], yh[U], yl[U], gs[U], mh[U], ml[U];
       int bq[U], iq[U];
       bool act[U];
+      // the pair's sources are read here, before any store of the batch, so that no shared
+      // memory store can stand between the arithmetic chains of the batch
 #pragma unroll
       for (int q = 0; q < U; ++q) {
-        const int pi = p0 + q;
-        const int b = pi < npairs ? pi / nrow : 0;
-        const int i = r0 + tid + (pi < npairs ? pi - b * nrow : 0) * KT;
+        const bool in = p0 + q < npairs;
+        const int b = in ? bc : 0;
+        const int i = r0 + tid + (in ? jc : 0) * KT;
+        if (in && ++jc == nrow) {
+          jc = 0;
+          ++bc;
+        }
         const SrcB& s = sb[b];
-        act[q] = pi < npairs && s.active;
+        act[q] = in && s.active;
         bq[q] = b;
         iq[q] = i;
+        mh[q] = s.m_hi;
+        ml[q] = s.m_lo;
         om[q] = yh[q] = yl[q] = gs[q] = 0.f;
         if (act[q]) {
           const size_t boff = ((size_t)s.base * B + b) * ld;
@@ -375,14 +386,14 @@ struct Engine {
       for (int q = 0; q < U; ++q) {
         if (!act[q]) continue;
         const int b = bq[q], i = iq[q];
-        const SrcB& s = sb[b];
-        const f2 pr = two_prod(om[q], s.m_hi);
+        const f2 pr = two_prod(om[q], mh[q]);
         const f2 s1 = two_sum(yh[q], pr.hi);
         const f2 s2 = two_sum(s1.hi, gs[q]);
-        const float lo = yl[q] + ((s1.lo + s2.lo) + __fmaf_rn(om[q], s.m_lo, pr.lo));
+        const float lo = yl[q] + ((s1.lo + s2.lo) + __fmaf_rn(om[q], ml[q], pr.lo));
         float sn, cs;
         sincos_pair(s2.hi, lo, &sn, &cs);
         xrow(b)[i] = make_float2(cs, sn);
+        const SrcB& s = sb[b];
         const bool emit = s.rec && emit_mode;
         if (s.store_y7 || emit) {
           const size_t boff = ((size_t)s.base * B + b) * ld;
@@ -642,6 +653,27 @@ struct Engine {
         const float c1 = tr[b].c1;
         float* gdst = s.gout >= 0 ? p.g + ((size_t)s.gout * B + b) * ld : nullptr;
         const bool rec = s.rec;
+        if (use_tab && !rec && gdst) {
+          // the common case, 4 rows at a time: every shared-memory read of the batch before
+          // its stores, which the compiler cannot reorder across
+          constexpr int U = 4;
+          for (int i0 = r0 + lt; i0 < r1; i0 += U * gt) {
+            float2 F[U], x[U];
+#pragma unroll
+            for (int q = 0; q < U; ++q) {
+              const int i = i0 + q * gt;
+              const bool ok = i < r1;
+              F[q] = ok ? tb[ubits[i - r0]] : make_float2(0.f, 0.f);
+              x[q] = ok ? xb[i] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int q = 0; q < U; ++q) {
+              const int i = i0 + q * gt;
+              if (i < r1) gdst[i] = c1 * (x[q].y * F[q].x - x[q].x * F[q].y);
+            }
+          }
+          continue;
+        }
         for (int i = r0 + lt; i < r1; i += gt) {
           const uint32_t u = ubits[i - r0];
           float Fc = 0.f, Fs = 0.f;
