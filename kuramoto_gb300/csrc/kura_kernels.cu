@@ -344,12 +344,21 @@ struct Engine {
   // projections and r sums from shared memory (the thread reads back its own rows).
   __device__ void phase_a_pairs(bool want_r, int npw) {
     const int ld = p.ld, k = p.k;
-    const int nrow = tid < r1 - r0 ? (r1 - r0 - tid + KT - 1) / KT : 0;
-    const int npairs = nrow * B;
     const bool emit_mode = (p.dense_level >= 1 && p.mode == MODE_INTEGRATE) || p.mode == MODE_FINAL;
+    // the (row, active trajectory) pairs of the CTA are dealt to its threads evenly (pair P =
+    // row + nrows * trajectory goes to thread P % KT), so no thread takes a third row of
+    // every trajectory while others take two; the slopes and phases a pair reads were written
+    // by other threads of the CTA
+    __syncthreads();
+    uint32_t actb = 0;
+    int nact = 0;
+    for (int b = 0; b < B; ++b)
+      if (sb[b].active) actb |= (uint32_t)b << (4 * nact++);
+    const int nrows = r1 - r0;
+    const int npairs = nrows * nact;
     constexpr int U = 4;
-    int bc = 0, jc = 0;  // (trajectory, row) of the next pair: pair p = b * nrow + j
-    for (int p0 = 0; p0 < npairs; p0 += U) {
+    int P = tid, bi = tid / nrows, rr = tid % nrows;
+    for (int p0 = tid; p0 < npairs; p0 += U * KT) {
       float om[U], yh[U], yl[U], gs[U], mh[U], ml[U];
       int bq[U], iq[U];
       bool act[U];
@@ -357,21 +366,23 @@ struct Engine {
       // memory store can stand between the arithmetic chains of the batch
 #pragma unroll
       for (int q = 0; q < U; ++q) {
-        const bool in = p0 + q < npairs;
-        const int b = in ? bc : 0;
-        const int i = r0 + tid + (in ? jc : 0) * KT;
-        if (in && ++jc == nrow) {
-          jc = 0;
-          ++bc;
+        const bool in = P < npairs;
+        const int b = in ? (int)((actb >> (4 * bi)) & 15u) : 0;
+        const int i = r0 + (in ? rr : 0);
+        P += KT;
+        rr += KT;
+        while (rr >= nrows) {
+          rr -= nrows;
+          ++bi;
         }
         const SrcB& s = sb[b];
-        act[q] = in && s.active;
+        act[q] = in;
         bq[q] = b;
         iq[q] = i;
         mh[q] = s.m_hi;
         ml[q] = s.m_lo;
         om[q] = yh[q] = yl[q] = gs[q] = 0.f;
-        if (act[q]) {
+        if (in) {
           const size_t boff = ((size_t)s.base * B + b) * ld;
           om[q] = p.omega[i];
           yh[q] = p.ph_hi[boff + i];
@@ -417,6 +428,7 @@ struct Engine {
         }
       }
     }
+    __syncthreads();  // pass 2 reads rows written by other threads
     for (int b = 0; b < B; ++b) {
       float acc[PW];
 #pragma unroll
