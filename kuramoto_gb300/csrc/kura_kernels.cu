@@ -77,8 +77,8 @@ __device__ __forceinline__ float4 ld_stream4(const float* p) {
 // ------------------------------------------------------------------ per-evaluation source
 // What one coupling evaluation integrates for one trajectory:
 //   theta = phase[base] + omega*(m_hi + m_lo) + sum_j W[j] * g[slot[j]]
-struct SrcB {
-  float W[7];
+struct __align__(16) SrcB {
+  float W[7];  // 16-byte aligned: read as two float4 (the second ends with E[0])
   float E[7];      // error weights h*e_j (error phase)
   float m_hi, m_lo;
   int slot[7];     // physical g slot of logical k_1..k_7
@@ -388,9 +388,17 @@ struct Engine {
           yh[q] = p.ph_hi[boff + i];
           yl[q] = p.ph_lo[boff + i];
           const int nW = s.nW;
+          // weights in two vector reads (W[7] is followed by E[0]); slopes 2..6 sit in their
+          // own slots, only k1 and k7 move (FSAL)
+          const float4 wa = *reinterpret_cast<const float4*>(&s.W[0]);
+          const float4 wb = *reinterpret_cast<const float4*>(&s.W[4]);
+          const float Wr[7] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z};
+          const int s0 = s.slot[0], s6 = s.slot[6];
 #pragma unroll
-          for (int j = 0; j < 7; ++j)
-            if (j < nW) gs[q] = __fmaf_rn(s.W[j], p.g[((size_t)s.slot[j] * B + b) * ld + i], gs[q]);
+          for (int j = 0; j < 7; ++j) {
+            const int sj = j == 0 ? s0 : (j == 6 ? s6 : j);
+            if (j < nW) gs[q] = __fmaf_rn(Wr[j], p.g[((size_t)sj * B + b) * ld + i], gs[q]);
+          }
         }
       }
 #pragma unroll
