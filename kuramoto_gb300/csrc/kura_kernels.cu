@@ -110,7 +110,7 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[4] = o; o += align16(sl * 4);                      // slice
   off[5] = o; o += align16(16 * 4);                      // flags
   off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
-  off[7] = o; o += align16(coup != KURA_COUPLING_VOLCANO ? bmax * (coup == COUP_DENSE_I8 && bmax == 1 ? CT_I8 : CT) * 8 : 0); // x tile
+  off[7] = o; o += align16(coup != KURA_COUPLING_VOLCANO ? bmax * (bmax == 1 ? (coup == COUP_DENSE_I8 ? CT_I8 : CT_F1) : CT) * 8 : 0); // x tile
   // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
   off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
   off[9] = o; o += align16(coup == KURA_COUPLING_VOLCANO && xs_smem ? bmax * rows * 8 : 0);  // own (cos, sin)
@@ -499,9 +499,14 @@ struct Engine {
     // own group of KW/B warps, so the trajectories of a batch proceed side by side.
     int b0, b1, lt, gt;
     work_map(b0, b1, lt, gt);
-    if (COUP == KURA_COUPLING_VOLCANO && xs != nullptr && all_warps_mode())
-      phase_a_pairs(want_r, npw);
-    else
+    bool paired = false;
+    if constexpr (COUP == KURA_COUPLING_VOLCANO) {
+      if (xs != nullptr && all_warps_mode()) {
+        phase_a_pairs(want_r, npw);
+        paired = true;
+      }
+    }
+    if (!paired)
     for (int b = b0; b < b1; ++b) {
       const SrcB& s = sb[b];
       float acc[PW];
@@ -742,6 +747,7 @@ struct Engine {
   // A (rows r0..r1 of this CTA) times the (cos, sin) of every trajectory.  x is
   // staged in shared memory one column tile at a time; each warp keeps RG rows in
   // flight, each lane reading 16-byte chunks of them.
+  static constexpr int CTF = BMAX == 1 ? CT_F1 : CT;  // columns per x tile of the float product
   __device__ void dense_matvec() {
     const int ld = p.ld;
     const int rows_per_pass = KW * RG;
@@ -753,12 +759,12 @@ struct Engine {
         for (int b = 0; b < BMAX; ++b) acc[q][b][0] = acc[q][b][1] = 0.f;
       // warp w takes rows pr0 + w + KW*q of the pass, so small row blocks keep every warp busy
       const int row0 = pr0 + warp;
-      for (int c0 = 0; c0 < ld; c0 += CT) {
+      for (int c0 = 0; c0 < ld; c0 += CTF) {
         __syncthreads();
-        const int cw = min(CT, ld - c0);
-        for (int t = tid; t < B * CT; t += KT) {
-          int b = t / CT, c = t - b * CT;
-          xt[b * CT + c] = (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
+        const int cw = min(CTF, ld - c0);
+        for (int t = tid; t < B * CTF; t += KT) {
+          int b = t / CTF, c = t - b * CTF;
+          xt[b * CTF + c] = (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
         }
         __syncthreads();
         for (int cc = lane * 4; cc < cw; cc += 128) {
@@ -771,7 +777,7 @@ struct Engine {
 #pragma unroll
           for (int b = 0; b < BMAX; ++b) {
             if (b < B) {
-              const float4* xp = reinterpret_cast<const float4*>(xt + b * CT + cc);
+              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTF + cc);
               float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
 #pragma unroll
               for (int q = 0; q < RG; ++q) {

@@ -10,6 +10,7 @@ constexpr int KT = 512;       // threads per CTA of the persistent integrator
 constexpr int KW = KT / 32;   // warps per CTA
 constexpr int CT = 1024;      // columns per staged x tile of the dense coupling
 constexpr int CT_I8 = 8192;   // the same for int8 rows and one trajectory (16 loads per lane per tile)
+constexpr int CT_F1 = 4096;   // the same for float rows and one trajectory
 constexpr int PW_MAX = 2 * 32 + 2;  // partial sums per trajectory and CTA: 2K projections + (sum cos, sum sin)
 
 // Per-trajectory scalars.  Every CTA keeps an identical copy in shared memory
