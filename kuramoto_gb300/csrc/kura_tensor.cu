@@ -558,7 +558,7 @@ int TensorEngine::init(int64_t n, int k, int batch, int seed, double atol, doubl
   Impl& I = *d;
   I.n = (int)n; I.K = k; I.B = batch; I.seed = seed; I.atol = atol; I.rtol = rtol; I.fixed = fixed;
   I.dense_level = dense_level; I.device = device; I.st = st;
-  I.np = (I.n + 127) / 128 * 128;
+  I.np = (I.n + 255) / 256 * 256;  // work units of two 128-row tiles
   I.bp = 16;
   while (I.bp < batch) I.bp *= 2;
   const size_t np = I.np, bp = I.bp;
@@ -593,7 +593,7 @@ int TensorEngine::init(int64_t n, int k, int batch, int seed, double atol, doubl
 }
 
 size_t TensorEngine::memory_required(int64_t n, int batch) {
-  size_t np = ((size_t)n + 127) / 128 * 128, bp = 16;
+  size_t np = ((size_t)n + 255) / 256 * 256, bp = 16;
   while ((int)bp < batch) bp *= 2;
   return np * np * 2 + np * bp * (2 * 16 + 7 * 4 + 4 * 2 + 8 + 4 + 8) + np * 4;
 }
@@ -703,23 +703,23 @@ static cudaError_t launch_gemm(TensorEngine::Impl& I, const TCoef* src, int mode
   constexpr int BP = NCOL / 4;  // trajectories per work unit
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, I.device);
-  const int mtiles = I.np / TG_BM, ktiles = I.np / TG_BK;
+  const int mtiles = I.np / (2 * TG_BM), ktiles = I.np / TG_BK;  // units of two row tiles
   const int nsplit = I.bp / BP, xstride = 4 * BP;
   const int grid = std::min(mtiles * nsplit, sms);
   const unsigned long long limit = 20000000000ull;
   if (I.has_lo) {
-    auto kl = k_tensor_gemm<NCOL / 2, LoEpi<BP>>;
-    cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL / 2>::SMEM);
+    auto kl = k_tensor_gemm<NCOL / 2, LoEpi<BP>, 2>;
+    cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL / 2, 2>::SMEM);
     LoEpi<BP> le{v, src};
-    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, ktiles, nsplit, xstride, le,
+    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2, 2>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, ktiles, nsplit, xstride, le,
                                                              I.err, limit, run_flag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  auto k = k_tensor_gemm<NCOL, KuraEpi<BP>>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL>::SMEM);
+  auto k = k_tensor_gemm<NCOL, KuraEpi<BP>, 2>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL, 2>::SMEM);
   KuraEpi<BP> ep{v, src, 1.0f / (float)I.n, I.has_lo ? 1 : 0};
-  k<<<grid, TG_THREADS, TGCfg<NCOL>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, ktiles, nsplit, xstride, ep, I.err, limit,
+  k<<<grid, TG_THREADS, TGCfg<NCOL, 2>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, ktiles, nsplit, xstride, ep, I.err, limit,
                                                    run_flag);
   return cudaGetLastError();
 }

@@ -21,32 +21,36 @@ constexpr int TG_BK = 32;   // K per stage (one 64-byte swizzle row of BF16)
 constexpr int TG_ROWB = TG_BK * 2;  // bytes per tile row
 constexpr int TG_THREADS = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 
-template <int NCOL> struct TGCfg {
+// NCOL columns per work unit, MT row tiles of 128 per work unit (sharing every X stage: MT = 2
+// halves the operand bytes per flop that X costs)
+template <int NCOL, int MT = 1> struct TGCfg {
   static constexpr int NMMA = NCOL > 256 ? 256 : NCOL;  // N of one MMA instruction
-  static constexpr int NH = NCOL / NMMA;                // MMAs per K step
-  static constexpr int A_BYTES = TG_BM * TG_BK * 2;
+  static constexpr int NH = NCOL / NMMA;                // MMAs per K step and row tile
+  static constexpr int A1_BYTES = TG_BM * TG_BK * 2;    // one row tile of a stage
+  static constexpr int A_BYTES = MT * A1_BYTES;
   static constexpr int X_BYTES = NCOL * TG_BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + X_BYTES;
   static constexpr int STAGES = (200 * 1024) / STAGE_BYTES > 8 ? 8 : (200 * 1024) / STAGE_BYTES;
-  static constexpr int ACC_COLS = NCOL < 32 ? 32 : NCOL;          // one accumulator
-  static constexpr int NACC = 2 * ACC_COLS <= 512 ? 2 : 1;          // double-buffered when TMEM allows
+  static constexpr int ACC_COLS = MT * NCOL < 32 ? 32 : MT * NCOL;  // one accumulator (all row tiles)
+  static constexpr int NACC = 2 * ACC_COLS <= 512 ? 2 : 1;           // double-buffered when TMEM allows
   static constexpr int TMEM_COLS = ACC_COLS * NACC;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
-  static_assert(NCOL % 16 == 0 && NCOL <= 512, "NCOL");
+  static_assert(NCOL % 16 == 0 && NCOL <= 512 && MT * NCOL <= 512, "NCOL");
   static_assert(STAGES >= 2, "stages");
 };
 
-// Work units: (128-row tile, column block); column block sp covers X rows
-// sp * xstride .. + NCOL.  Epilogue interface: Epi::row(taddr, row, m0, sp) is called by
+// Work units: (MT row tiles of 128, column block); column block sp covers X rows
+// sp * xstride .. + NCOL; mtiles counts units of MT * 128 rows.  Epilogue interface:
+// Epi::row(taddr, row, m0, sp) is called by
 // every thread of warps 1-4 with taddr = TMEM address of this thread's accumulator row
 // (lane field set, column 0).  With NCOL <= 256 the accumulator is double-buffered in TMEM,
 // so one unit's epilogue overlaps the next unit's MMAs.
-template <int NCOL, class Epi>
+template <int NCOL, class Epi, int MT = 1>
 __global__ void __launch_bounds__(TG_THREADS, 1)
     k_tensor_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int mtiles,
                   int ktiles, int nsplit, int xstride, Epi epi, int* err, unsigned long long limit_ns,
                   const int* run_flag) {
-  using C = TGCfg<NCOL>;
+  using C = TGCfg<NCOL, MT>;
   if (run_flag && *run_flag == 0) return;  // nothing to compute (every column inactive)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -96,7 +100,9 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
           }
           unsigned char* st = smem + s * C::STAGE_BYTES;
           umma::mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
-          umma::tma_load_2d(st, &tmA, &full[s], kt * TG_BK, tile * TG_BM);
+#pragma unroll
+          for (int mt = 0; mt < MT; ++mt)
+            umma::tma_load_2d(st + mt * C::A1_BYTES, &tmA, &full[s], kt * TG_BK, (tile * MT + mt) * TG_BM);
 #pragma unroll
           for (int h = 0; h < (NCOL + 255) / 256; ++h)
             umma::tma_load_2d(st + C::A_BYTES + h * 256 * TG_ROWB, &tmX, &full[s], kt * TG_BK, xr0 + h * 256);
@@ -139,11 +145,14 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
           const uint32_t x0 = a0 + C::A_BYTES;
 #pragma unroll
           for (int kk = 0; kk < TG_BK / 16; ++kk) {
-            const uint64_t ad = umma::sw64_desc(a0 + kk * 32);
 #pragma unroll
-            for (int h = 0; h < C::NH; ++h) {
-              const uint64_t xd = umma::sw64_desc(x0 + h * C::NMMA * TG_ROWB + kk * 32);
-              umma::mma_bf16(tacc + h * C::NMMA, ad, xd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+            for (int mt = 0; mt < MT; ++mt) {
+              const uint64_t ad = umma::sw64_desc(a0 + mt * C::A1_BYTES + kk * 32);
+#pragma unroll
+              for (int h = 0; h < C::NH; ++h) {
+                const uint64_t xd = umma::sw64_desc(x0 + h * C::NMMA * TG_ROWB + kk * 32);
+                umma::mma_bf16(tacc + mt * NCOL + h * C::NMMA, ad, xd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
+              }
             }
           }
           umma::mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
@@ -166,7 +175,10 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
       }
       umma::tc_fence_after();
       const int row = q * 32 + lane;
-      epi.row(tmem + buf * C::ACC_COLS + ((uint32_t)(q * 32) << 16), row, (u / nsplit) * TG_BM, u % nsplit);
+#pragma unroll 1
+      for (int mt = 0; mt < MT; ++mt)
+        epi.row(tmem + buf * C::ACC_COLS + mt * NCOL + ((uint32_t)(q * 32) << 16), row,
+                ((u / nsplit) * MT + mt) * TG_BM, u % nsplit);
       umma::tc_fence_before();
       __syncwarp();
       if (lane == 0) umma::mbar_arrive(&accempty[buf]);
