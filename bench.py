@@ -365,7 +365,8 @@ def run_multi(args, w):
     res = dict(value=units / (ms / 1e3), ms=ms, kernel_ms=kern_ms, launches=args.steps,
                e2e_value=e2e_units / (e2e_ms / 1e3), h2d=8 * tot, d2h=4 * order.size + 4 * tot + 8 * len(ns),
                clocks=clk.summary(), orders=order, nets=nets, osc_per_step=osc / args.steps,
-               shape=(st["cluster_size"], st["block_threads"], st["grid"]), tune_ms=st["tune_ms"], acc=acc)
+               shape=(st["cluster_size"], st["block_threads"], st["grid"], st["heavy"]), tune_ms=st["tune_ms"],
+               acc=acc)
     m.close()
     return res
 
@@ -461,7 +462,8 @@ def main_multi(args, w):
                         "kernel_ms_per_launch": round(res["kernel_ms"] / args.steps, 3)}
     line["clocks"] = res["clocks"]
     line["launch_shape"] = {"cluster_size": res["shape"][0], "block_threads": res["shape"][1],
-                            "grid": res["shape"][2], "autotune_trial_ms": round(res["tune_ms"], 3)}
+                            "grid": res["shape"][2], "heavy_networks_in_large_clusters": res["shape"][3],
+                            "autotune_trial_ms": round(res["tune_ms"], 3)}
     line["accepted_steps_per_network"] = {"mean": float(res["acc"].mean()), "max": int(res["acc"].max())}
     if not args.no_cpu:
         v, el, osc = multi_cpu(w, res["nets"], threads, MULTI_CPU_T1)

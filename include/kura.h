@@ -191,8 +191,8 @@ typedef struct kura_multi_stats {
   int64_t rejected;     /* rejected attempts, all networks */
   int32_t cluster_size; /* CTAs per network */
   int32_t block_threads;
-  int32_t grid; /* CTAs launched */
-  int32_t reserved;
+  int32_t grid;  /* CTAs of the main launch */
+  int32_t heavy; /* networks run in large clusters beside the main launch */
 } kura_multi_stats;
 
 typedef struct kura_multi kura_multi;

@@ -18,8 +18,9 @@
 // exchanging them, and every cluster barrier is reached by all of them.
 //
 // The launch shape (cluster size, block size) comes from an autotuner that times a
-// stratified sample of the networks at every candidate shape; the queue reset and the
-// persistent launch are captured in a CUDA graph that every integration replays.
+// stratified sample of the networks at every candidate shape.  An integration is a pilot
+// launch (a CUDA graph replayed every time) followed by the rest of the work in the order
+// of predicted cost, the heaviest networks in large clusters beside the others.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <algorithm>
@@ -521,14 +522,17 @@ struct kura_multi {
   bool tuned = false;
   std::vector<MInst> queue;  // largest network first
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;  // the heavy networks' launch, beside the main one
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t evf = nullptr, evj = nullptr;  // fork after the pilot, join of the heavy launch
+  MInst* d_instH = nullptr;
+  int heavy = 0, heavy_cs = 0;
   MInst* d_inst = nullptr;
   int *d_queue = nullptr, *d_status = nullptr;
   float *d_om = nullptr, *d_th = nullptr, *d_hi = nullptr, *d_lo = nullptr, *d_g = nullptr, *d_r = nullptr,
         *d_theta = nullptr;
   long long *d_w = nullptr, *d_acc = nullptr, *d_rej = nullptr;
   cudaGraphExec_t graph = nullptr;   // pilot: every network's first attempts, in size order
-  cudaGraphExec_t graph2 = nullptr;  // the rest, longest predicted work first
   kura::MNet* d_state = nullptr;
   MInst* d_inst2 = nullptr;
   int pilot_attempts = 32;
@@ -653,10 +657,12 @@ cudaError_t capture(kura_multi* m, const MParams& p, bool reset_state, cudaGraph
   return e;
 }
 
-// two launches per integration: a pilot runs the first attempts of every network (largest
-// first); the host then orders the unfinished networks by their predicted remaining work,
-// (t1 - t) / h steps of (N + 2048) row-equivalents each, and the second launch runs them in
-// that order, so the networks with the most steps start first (longest-processing-time)
+// The pilot launch runs the first attempts of every network (largest first) and is
+// captured in a CUDA graph.  The host then orders the unfinished networks by their
+// predicted remaining work, (t1 - t) / h steps of (N + 2048) row-equivalents each, and
+// launches the rest in that order (longest-processing-time first): the few networks whose
+// work alone exceeds a cluster's fair share go to large clusters on a second stream, the
+// others to the autotuned shape.
 int build_graph(kura_multi* m) {
   MParams p = base_params(m);
   p.rows_max = (m->maxn + m->cs - 1) / m->cs;
@@ -664,11 +670,6 @@ int build_graph(kura_multi* m) {
   MCU(cudaStreamSynchronize(m->st));
   p.max_attempts = m->pilot_attempts;
   cudaError_t e = capture(m, p, true, &m->graph);
-  if (e == cudaSuccess) {
-    p.max_attempts = -1;
-    p.inst = m->d_inst2;
-    e = capture(m, p, false, &m->graph2);
-  }
   if (e != cudaSuccess)
     return mfail(KURA_ERR_CUDA, std::string("capturing the multi-network launches: ") + cudaGetErrorString(e));
   return KURA_OK;
@@ -745,7 +746,7 @@ extern "C" int kura_multi_create(const kura_instance* inst, int32_t count, doubl
     void** p;
     size_t bytes;
   } allocs[] = {
-      {(void**)&m->d_inst, sizeof(MInst) * count}, {(void**)&m->d_queue, sizeof(int)},
+      {(void**)&m->d_inst, sizeof(MInst) * count}, {(void**)&m->d_queue, 2 * sizeof(int)},
       {(void**)&m->d_status, sizeof(int) * count}, {(void**)&m->d_om, sizeof(float) * T},
       {(void**)&m->d_th, sizeof(float) * T},       {(void**)&m->d_hi, sizeof(float) * 2 * T},
       {(void**)&m->d_lo, sizeof(float) * 2 * T},   {(void**)&m->d_w, sizeof(long long) * 2 * T},
@@ -753,6 +754,7 @@ extern "C" int kura_multi_create(const kura_instance* inst, int32_t count, doubl
       {(void**)&m->d_theta, sizeof(float) * T},    {(void**)&m->d_acc, sizeof(long long) * count},
       {(void**)&m->d_rej, sizeof(long long) * count},
       {(void**)&m->d_state, sizeof(kura::MNet) * count}, {(void**)&m->d_inst2, sizeof(MInst) * count},
+      {(void**)&m->d_instH, sizeof(MInst) * count},
   };
   for (auto& a : allocs) {
     e = cudaMalloc(a.p, a.bytes);
@@ -761,6 +763,9 @@ extern "C" int kura_multi_create(const kura_instance* inst, int32_t count, doubl
                              std::string("device allocation: ") + cudaGetErrorString(e)));
   }
   e = cudaStreamCreateWithFlags(&m->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->st2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->evf, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&m->evj, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&m->ev[0]);
   if (e == cudaSuccess) e = cudaEventCreate(&m->ev[1]);
   if (e != cudaSuccess) return fail_free(mfail(KURA_ERR_CUDA, cudaGetErrorString(e)));
@@ -773,14 +778,19 @@ extern "C" void kura_multi_destroy(kura_multi* m) {
   cudaSetDevice(m->device);
   if (m->st) cudaStreamSynchronize(m->st);
   if (m->graph) cudaGraphExecDestroy(m->graph);
-  if (m->graph2) cudaGraphExecDestroy(m->graph2);
   void* ptrs[] = {m->d_inst, m->d_queue, m->d_status, m->d_om,    m->d_th,    m->d_hi,    m->d_lo,
                   m->d_w,    m->d_g,     m->d_r,      m->d_theta, m->d_acc,   m->d_rej,   m->d_state,
-                  m->d_inst2};
+                  m->d_inst2, m->d_instH};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t v : m->ev)
     if (v) cudaEventDestroy(v);
+  if (m->evf) cudaEventDestroy(m->evf);
+  if (m->evj) cudaEventDestroy(m->evj);
+  if (m->st2) {
+    cudaStreamSynchronize(m->st2);
+    cudaStreamDestroy(m->st2);
+  }
   if (m->st) cudaStreamDestroy(m->st);
   delete m;
 }
@@ -825,8 +835,57 @@ extern "C" int kura_multi_integrate(kura_multi* m, const float* omega, const flo
   });
   std::vector<MInst> order2(m->count);
   for (int q = 0; q < m->count; ++q) order2[q] = m->queue[cost[q].second];
-  MCU(cudaMemcpyAsync(m->d_inst2, order2.data(), sizeof(MInst) * m->count, cudaMemcpyHostToDevice, m->st));
-  MCU(cudaGraphLaunch(m->graph2, m->st));
+  // Networks whose predicted work alone exceeds a cluster's fair share of the main launch
+  // (at most 4) run in a launch of their own with clusters of 1024-thread CTAs, started
+  // first on a second stream so that its CTAs take whole SMs; the main launch fills the
+  // rest.  Such a network sets the end of the run, and its time is bound by the latency of
+  // one step rather than by the SMs it holds.
+  double total = 0;
+  for (const auto& c : cost) total += c.first;
+  const double share = total / std::max(1, m->grid / m->cs);
+  int nh = 0;
+  while (nh < m->count && nh < 4 && cost[nh].first > share) ++nh;
+  int hcs = 0;
+  if (nh > 0) {
+    int maxnH = 0;
+    for (int q = 0; q < nh; ++q) maxnH = std::max(maxnH, order2[q].n);
+    int want = 2;
+    while (want < 16 && want * 2048 < maxnH) want *= 2;
+    MCU(cudaMemcpyAsync(m->d_instH, order2.data(), sizeof(MInst) * nh, cudaMemcpyHostToDevice, m->st));
+    MCU(cudaEventRecord(m->evf, m->st));
+    MCU(cudaStreamWaitEvent(m->st2, m->evf, 0));
+    MCU(cudaMemsetAsync(m->d_queue + 1, 0, sizeof(int), m->st2));
+    MParams ph = base_params(m);
+    ph.inst = m->d_instH;
+    ph.count = nh;
+    ph.queue = m->d_queue + 1;
+    for (int c = want; c >= 2 && !hcs; c /= 2) {
+      ph.rows_max = (maxnH + c - 1) / c;
+      if ((size_t)ph.rows_max * kura::M_ROW_BYTES > (size_t)kura::M_SMEM_CAP) break;
+      if (kura::launch_multi(ph, c, 1024, m->st2, nullptr) == cudaSuccess)
+        hcs = c;
+      else
+        cudaGetLastError();  // cluster shape not available: try a smaller one
+    }
+    if (hcs) {
+      MCU(cudaEventRecord(m->evj, m->st2));
+    } else {
+      nh = 0;
+    }
+  }
+  m->heavy = nh;
+  m->heavy_cs = hcs;
+  MCU(cudaMemcpyAsync(m->d_inst2, order2.data() + nh, sizeof(MInst) * (m->count - nh), cudaMemcpyHostToDevice,
+                      m->st));
+  {
+    MParams p2 = base_params(m);
+    p2.inst = m->d_inst2;
+    p2.count = m->count - nh;
+    p2.rows_max = (m->maxn + m->cs - 1) / m->cs;
+    MCU(cudaMemsetAsync(m->d_queue, 0, sizeof(int), m->st));
+    if (p2.count > 0) MCU(kura::launch_multi(p2, m->cs, m->nt, m->st, nullptr));
+  }
+  if (nh > 0) MCU(cudaStreamWaitEvent(m->st, m->evj, 0));
   MCU(cudaEventRecord(m->ev[1], m->st));
   const size_t rec = (size_t)m->count * (m->n_eval + 1);
   MCU(cudaMemcpyAsync(order, m->d_r, sizeof(float) * rec, cudaMemcpyDeviceToHost, m->st));
@@ -845,6 +904,7 @@ extern "C" int kura_multi_integrate(kura_multi* m, const float* omega, const flo
   s.cluster_size = m->cs;
   s.block_threads = m->nt;
   s.grid = m->grid;
+  s.heavy = m->heavy;
   s.accepted = s.rejected = 0;
   s.osc_steps = 0;
   int bad = -1;

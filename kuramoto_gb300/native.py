@@ -59,7 +59,7 @@ class MultiStats(ctypes.Structure):
     _fields_ = [
         ("kernel_ms", ctypes.c_double), ("osc_steps", ctypes.c_double), ("tune_ms", ctypes.c_double),
         ("accepted", ctypes.c_int64), ("rejected", ctypes.c_int64), ("cluster_size", ctypes.c_int32),
-        ("block_threads", ctypes.c_int32), ("grid", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("block_threads", ctypes.c_int32), ("grid", ctypes.c_int32), ("heavy", ctypes.c_int32),
     ]
 
 
