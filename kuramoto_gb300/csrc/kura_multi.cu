@@ -85,11 +85,13 @@ struct MNet {
 
 struct MSmem {
   float red[32][M_NV];
-  float part[2][M_NV];  // this CTA's totals by reduction parity (read by the cluster)
+  float part[2][M_MAX_CLUSTER][M_NV];  // every CTA's totals by reduction parity and rank
   float rsum[M_NV];
+  float f3[2 * M_KMAX];  // (-1)^m / N times the projection totals
   float2 tab[256];  // sum_m +-f3_m for every sign pattern of the K factor bits
-  float W[8], E[8];
-  float mh, ml;
+  float E[8];           // error weights of the attempt
+  float Wst[7][8];      // rows 0..5: weights h a_sj of stages 2..7; row 6: dense output
+  float mhs[7], mls[7];  // the time offset of each row as a float pair
   int idx;
   double t, h, t_last;
   long long acc, rej;
@@ -171,24 +173,29 @@ struct Multi {
     if (mine) {
       float s = 0.f;
       for (int q = 0; q < NW; ++q) s += S.red[q][tid];
-      S.part[par][tid] = s;
+      // pushed into slot `rank` of every CTA of the cluster, so that the totals are read
+      // from local shared memory after the barrier
+      for (int r = 0; r < CS; ++r) cl.map_shared_rank(&S.part[par][0][0], r)[rank * M_NV + tid] = s;
     }
     cl.sync();  // every CTA's totals are visible
     if (mine) {
       float s = 0.f;
-      for (int r = 0; r < CS; ++r) s += cl.map_shared_rank(&S.part[par][0], r)[tid];
+      for (int r = 0; r < CS; ++r) s += S.part[par][r][tid];
       S.rsum[tid] = s;
+      if (tid < nproj) S.f3[tid] = (((tid >> 1) & 1) ? -s : s) / (float)n;
     }
-    // the other parity is free: every CTA finished reading it before this barrier
+    // a CTA writes into this parity's slots again two reductions later, after the barrier
+    // of the next one, which every CTA reaches only after reading these totals
     par ^= 1;
     __syncthreads();
   }
 
-  // one coupling evaluation at theta = y[base] + omega*(mh+ml) + sum_j W_j g_j (a stage
-  // argument, dp45.cu:90-106, or the dense output, dp45.cu:70-76).  Writes g[gout] =
+  // one coupling evaluation at theta = y[base] + omega*(mh+ml) + sum_j W_j g_j with the
+  // weights of row si (a stage argument, dp45.cu:90-106, or the dense output,
+  // dp45.cu:70-76).  Writes g[gout] =
   // c (sin F_c - cos F_s) (kuramoto.cu:104-126) when gout >= 0 and the r sums when
   // want_r; store_y7 keeps the stage-7 argument (FSAL) as the next y
-  __device__ void coupling(int base, int nW, int g1, int gout, bool want_r, bool store_y7) {
+  __device__ void coupling(int base, int si, int nW, int g1, int gout, bool want_r, bool store_y7) {
     float acc[M_NV];
 #pragma unroll
     for (int v = 0; v < M_NV; ++v) acc[v] = 0.f;
@@ -198,11 +205,11 @@ struct Multi {
       const long long gi = off + i;
       const float om = p.omega[gi];
       float gsum = 0.f;
-      for (int j = 0; j < nW; ++j) gsum = __fmaf_rn(S.W[j], p.g[(long long)slot_of(j, g1) * T + gi], gsum);
-      const f2 pr = two_prod(om, S.mh);
+      for (int j = 0; j < nW; ++j) gsum = __fmaf_rn(S.Wst[si][j], p.g[(long long)slot_of(j, g1) * T + gi], gsum);
+      const f2 pr = two_prod(om, S.mhs[si]);
       const f2 s1 = two_sum(p.ph_hi[base * T + gi], pr.hi);
       const f2 s2 = two_sum(s1.hi, gsum);
-      const float lo = p.ph_lo[base * T + gi] + ((s1.lo + s2.lo) + __fmaf_rn(om, S.ml, pr.lo));
+      const float lo = p.ph_lo[base * T + gi] + ((s1.lo + s2.lo) + __fmaf_rn(om, S.mls[si], pr.lo));
       float sn, cs;
       sincos_pair(s2.hi, lo, &sn, &cs);
       xs[i - r0] = make_float2(cs, sn);
@@ -244,8 +251,7 @@ struct Multi {
     for (int pat = tid; pat < (1 << k); pat += NT) {
       float Fc = 0.f, Fs = 0.f;
       for (int m = 0; m < k; ++m) {
-        const float sgn = (m & 1) ? -1.f : 1.f;
-        const float fc = (sgn * S.rsum[2 * m]) / (float)n, fs = (sgn * S.rsum[2 * m + 1]) / (float)n;
+        const float fc = S.f3[2 * m], fs = S.f3[2 * m + 1];
         const bool pos = (pat >> m) & 1;
         Fc += pos ? fc : -fc;
         Fs += pos ? fs : -fs;
@@ -258,6 +264,26 @@ struct Multi {
       const float2 F = S.tab[ubits[i - r0]];
       const float2 x = xs[i - r0];
       gdst[i] = c1 * (x.y * F.x - x.x * F.y);
+    }
+  }
+
+  // the stage and error weights of the next attempt from S.h (dp45.cu:90-106, 116), by
+  // the lanes of warp 0 in parallel
+  __device__ void fill_stage_tables() {
+    const double h = S.h;
+    for (int e = lane; e < 6 * 8 + 6 + 7; e += 32) {
+      if (e < 48) {
+        const int s = 2 + e / 8, j = e % 8;
+        S.Wst[s - 2][j] = (j < s - 1) ? (float)(h * A_TAB[s - 1][j]) : 0.f;
+      } else if (e < 54) {
+        const int s = 2 + (e - 48);
+        const double mh = C_TAB[s - 1] * h;
+        const float hi = (float)mh;
+        S.mhs[s - 2] = hi;
+        S.mls[s - 2] = (float)(mh - (double)hi);
+      } else {
+        S.E[e - 54] = (float)(h * E_TAB[e - 54]);
+      }
     }
   }
 
@@ -317,12 +343,16 @@ struct Multi {
         S.eval_end = G.eval_end;
         S.status = G.status;
       }
-      S.mh = S.ml = 0.f;
+      S.mhs[6] = S.mls[6] = 0.f;
+    }
+    if (warp == 0) {
+      __syncwarp();
+      fill_stage_tables();
     }
     __syncthreads();
     if (stage == 0) {
       // first slope of the run (dp45.cu:151) and the record at t = 0
-      coupling(0, 0, 0, 0, true, false);
+      coupling(0, 6, 0, 0, 0, true, false);
       record(I, 0);
     }
     long long attempts = 0;
@@ -336,13 +366,13 @@ struct Multi {
           const double hs = S.t - S.t_last, dl = te - S.t_last, x = dl / hs;
           for (int j = 0; j < 7; ++j) {
             const double cc = ((P_TAB[j][3] * x + P_TAB[j][2]) * x + P_TAB[j][1]) * x * x + P_TAB[j][0] * x;
-            S.W[j] = (float)(hs * cc);
+            S.Wst[6][j] = (float)(hs * cc);
           }
-          S.mh = (float)dl;
-          S.ml = (float)(dl - (double)S.mh);
+          S.mhs[6] = (float)dl;
+          S.mls[6] = (float)(dl - (double)S.mhs[6]);
         }
         __syncthreads();
-        coupling(S.rot_y ^ 1, 7, S.rot_g ? 0 : 6, -1, true, false);
+        coupling(S.rot_y ^ 1, 6, 7, S.rot_g ? 0 : 6, -1, true, false);
         record(I, 1 + S.eval_i);
         __syncthreads();  // every thread has read eval_i
         if (tid == 0) S.eval_i++;
@@ -352,22 +382,13 @@ struct Multi {
       if (!(S.t < p.t1) || S.status != 0) break;
       if (p.max_attempts >= 0 && attempts >= p.max_attempts) break;
       attempts++;
-      // one attempt (dp45_step, dp45.cu:87-141)
+      // one attempt (dp45_step, dp45.cu:87-141).  The weights were filled after the last
+      // controller decision; stage s + 1 needs no barrier of its own after stage s, because
+      // every thread reads and writes the same rows in every stage and the shared buffers
+      // of the reduction and the table are ordered by the barriers inside the reduction
       const int g1 = S.rot_g ? 6 : 0;
-      for (int s = 2; s <= 7; ++s) {
-        if (tid == 0) {
-          const double h = S.h;
-          for (int j = 0; j < 7; ++j) S.W[j] = (j < s - 1) ? (float)(h * A_TAB[s - 1][j]) : 0.f;
-          const double mh = C_TAB[s - 1] * h;
-          S.mh = (float)mh;
-          S.ml = (float)(mh - (double)S.mh);
-          if (s == 7)
-            for (int j = 0; j < 7; ++j) S.E[j] = (float)(h * E_TAB[j]);
-        }
-        __syncthreads();
-        coupling(S.rot_y, s - 1, g1, s < 7 ? s - 1 : 6 - g1, false, s == 7);
-        __syncthreads();  // S.W is rewritten for the next stage
-      }
+      for (int s = 2; s <= 7; ++s)
+        coupling(S.rot_y, s - 2, s - 1, g1, s < 7 ? s - 1 : 6 - g1, false, s == 7);
       // error norm sqrt(sum (err_i / tol_i)^2 / N) (dp45.cu:79-84, 116-119); the omega
       // parts of the slopes cancel in the error weights
       float e2[M_NV];
@@ -414,6 +435,10 @@ struct Multi {
             if (!(S.h >= 1e-14 * fmax(1.0, fabs(S.t)))) S.status = KURA_ERR_STEP_UNDERFLOW;
           }
         }
+      }
+      if (warp == 0) {
+        __syncwarp();
+        fill_stage_tables();
       }
       __syncthreads();
     }
