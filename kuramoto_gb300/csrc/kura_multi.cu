@@ -24,6 +24,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -81,7 +83,14 @@ struct MNet {
   double t, h, t_last;
   long long acc, rej;
   int rot_y, rot_g, eval_i, eval_end, status, stage;
+  unsigned long long ns;  // time the network has spent in its clusters (the autotuner reads it)
 };
+
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 struct MSmem {
   float red[32][M_NV];
@@ -96,6 +105,7 @@ struct MSmem {
   double t, h, t_last;
   long long acc, rej;
   int rot_y, rot_g, eval_i, eval_end, status;
+  unsigned long long t_start;  // when the cluster took the network (rank 0)
 };
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -305,6 +315,7 @@ struct Multi {
     MNet& G = p.state[I.id];
     const int stage = G.stage;  // the same on every CTA of the cluster
     if (stage == 2) return;     // finished by an earlier launch
+    if (rank == 0 && tid == 0) S.t_start = now_ns();
     // factor bits (low bit of Philox element m*N + i, kuramoto.cu:128-135) and, on a fresh
     // start, y(0)
     for (int i = r0 + tid; i < r1; i += NT) {
@@ -462,6 +473,7 @@ struct Multi {
       G.eval_end = S.eval_end;
       G.status = S.status;
       G.stage = finished ? 2 : 1;
+      G.ns += now_ns() - S.t_start;
       p.accepted[I.id] = S.acc;
       p.rejected[I.id] = S.rej;
       p.status[I.id] = finished ? (S.status == 0 ? 1 : S.status) : 0;
@@ -522,6 +534,40 @@ cudaError_t launch_multi_t(const MParams& p, int cs, cudaStream_t st, int* grid_
   cfg.gridDim = dim3(clusters * cs);
   if (grid_out) *grid_out = clusters * cs;
   return cudaLaunchKernelEx(&cfg, f, p);
+}
+
+template <int NT>
+cudaError_t clusters_t(int cs, int rows, int* out) {
+  auto f = k_multi<NT>;
+  const size_t smem = dyn_smem(rows);
+  cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (cs > 8) {
+    e = cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3(cs);
+  return cudaOccupancyMaxActiveClusters(out, (void*)f, &cfg);
+}
+
+// clusters of `cs` CTAs of `nt` threads with `rows` rows each that fit on the GPU at once
+cudaError_t clusters_of(int cs, int nt, int rows, int* out) {
+  switch (nt) {
+    case 256: return clusters_t<256>(cs, rows, out);
+    case 512: return clusters_t<512>(cs, rows, out);
+    case 1024: return clusters_t<1024>(cs, rows, out);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_multi(const MParams& p, int cs, int nt, cudaStream_t st, int* grid) {
@@ -607,8 +653,16 @@ MParams base_params(kura_multi* m) {
   return p;
 }
 
-// time a bounded run of a stratified sample of the networks at every candidate shape and
-// keep the one with the most oscillator-attempts per second
+// Runs a stratified sample of the networks for a few attempts at every candidate shape and
+// keeps the one with the shortest predicted integration.  A network's predicted time is its
+// predicted step count, (t1 - t) / h after the trial, times the time per attempt it took in
+// this shape.  The prediction for the shape is the larger of the balanced total (the sum over
+// the networks, scaled to all of them, over the clusters) and twice the longest network.
+// Step counts are heavy-tailed (they grow with a network's fastest oscillator and with its
+// coupling as it synchronises), so the latency of one network's step often decides; the
+// factor 2 is there because the first attempts underestimate the longest networks the most
+// (on 512 networks with Cauchy frequencies they predicted 1/5 of the total step count and
+// 1/11 of the longest network's).  KURA_MULTI_TUNE_LOG=1 prints every trial's figures.
 int autotune(kura_multi* m) {
   const int S = std::min(m->count, 2 * 152);
   std::vector<MInst> sample(S);
@@ -626,6 +680,9 @@ int autotune(kura_multi* m) {
   q.max_attempts = 24;
   double best = -1;
   float best_ms = 0;
+  std::vector<kura::MNet> st(S);
+  const char* env = std::getenv("KURA_MULTI_TUNE_LOG");  // "1": print every trial's prediction
+  const bool tune_log = env && env[0] == '1';
   const int css[] = {1, 2, 4, 8, 16};
   const int nts[] = {256, 512, 1024};
   for (int c : css) {
@@ -645,14 +702,29 @@ int autotune(kura_multi* m) {
       MCU(cudaStreamSynchronize(m->st));
       float ms = 0;
       MCU(cudaEventElapsedTime(&ms, m->ev[0], m->ev[1]));
-      std::vector<long long> acc(S), rej(S);
-      MCU(cudaMemcpy(acc.data(), m->d_acc, sizeof(long long) * S, cudaMemcpyDeviceToHost));
-      MCU(cudaMemcpy(rej.data(), m->d_rej, sizeof(long long) * S, cudaMemcpyDeviceToHost));
-      double work = 0;
-      for (int i = 0; i < S; ++i) work += (double)(acc[i] + rej[i]) * sample[i].n;
-      const double rate = work / std::max(ms, 1e-3f);
-      if (rate > best) {
-        best = rate;
+      MCU(cudaMemcpy(st.data(), m->d_state, sizeof(kura::MNet) * S, cudaMemcpyDeviceToHost));
+      int fit = 0;
+      if (kura::clusters_of(c, t, q.rows_max, &fit) != cudaSuccess || fit < 1) {
+        cudaGetLastError();
+        continue;
+      }
+      double total = 0, longest = 0;
+      for (int i = 0; i < S; ++i) {
+        const kura::MNet& G = st[i];
+        const long long att = G.acc + G.rej;
+        if (att < 1) continue;
+        const double per = (double)G.ns / (double)att;
+        const double steps = G.stage == 2 ? 0.0 : std::max(0.0, m->t1 - G.t) / std::max(G.h, 1e-300);
+        total += steps * per;
+        longest = std::max(longest, steps * per);
+      }
+      const double balanced = total * ((double)m->count / S) / std::min(fit, m->count);
+      const double est = std::max(balanced, 2.0 * longest);
+      if (tune_log)
+        std::fprintf(stderr, "kura_multi autotune: cluster %d x %d threads, %d clusters, trial %.3f ms, "
+                     "balanced %.3f s, longest %.3f s\n", c, t, fit, ms, balanced * 1e-9, longest * 1e-9);
+      if (best < 0 || est < best) {
+        best = est;
         best_ms = ms;
         m->cs = c;
         m->nt = t;
