@@ -656,8 +656,9 @@ MParams base_params(kura_multi* m) {
 // Runs a stratified sample of the networks for a few attempts at every candidate shape and
 // keeps the one with the shortest predicted integration.  A network's predicted time is its
 // predicted step count, (t1 - t) / h after the trial, times the time per attempt it took in
-// this shape.  The prediction for the shape is the larger of the balanced total (the sum over
-// the networks, scaled to all of them, over the clusters) and twice the longest network.
+// this shape.  The prediction for the shape is the trial's time scaled to all networks (the
+// first attempts of every network) plus the larger of the balanced total (the sum over the
+// networks, scaled to all of them, over the clusters) and twice the longest network.
 // Step counts are heavy-tailed (they grow with a network's fastest oscillator and with its
 // coupling as it synchronises), so the latency of one network's step often decides; the
 // factor 2 is there because the first attempts underestimate the longest networks the most
@@ -719,10 +720,12 @@ int autotune(kura_multi* m) {
         longest = std::max(longest, steps * per);
       }
       const double balanced = total * ((double)m->count / S) / std::min(fit, m->count);
-      const double est = std::max(balanced, 2.0 * longest);
+      const double first = (double)ms * 1e6 * ((double)m->count / S);  // the trial's attempts for all
+      const double est = first + std::max(balanced, 2.0 * longest);
       if (tune_log)
         std::fprintf(stderr, "kura_multi autotune: cluster %d x %d threads, %d clusters, trial %.3f ms, "
-                     "balanced %.3f s, longest %.3f s\n", c, t, fit, ms, balanced * 1e-9, longest * 1e-9);
+                     "balanced %.3f s, longest %.3f s, predicted %.3f s\n", c, t, fit, ms, balanced * 1e-9,
+                     longest * 1e-9, est * 1e-9);
       if (best < 0 || est < best) {
         best = est;
         best_ms = ms;
