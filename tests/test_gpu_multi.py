@@ -154,3 +154,34 @@ def test_errors(native):
         with pytest.raises(native.KuraError) as e:
             m.integrate(om, th)
     assert e.value.code == -5
+
+
+def test_heavy_network_runs_beside_the_main_launch(native, oracle_lib):
+    """One network whose predicted work dwarfs the others' (a Cauchy outlier of |omega| ~ 1e3
+    among small normal-frequency networks) is moved to a launch of its own in large clusters
+    on a second stream.  Its records match the FP64 oracle, match the same network run alone
+    to rounding, and a second integration is bitwise identical."""
+    ns, ks, seeds, cs, ths, oms = networks(24, 31, 200, 600, kind="normal")
+    th_h, om_h = normal_inputs(3000, 4242, init=2 * np.pi)
+    om_h[17] = np.float32(1.2e3)  # one fast oscillator sets the step of the whole network
+    ns = np.concatenate([ns, [3000]])
+    ks = np.concatenate([ks, [5]])
+    seeds = np.concatenate([seeds, [77]])
+    cs = np.concatenate([cs, np.float32([4.0])]).astype(np.float32)
+    ths, oms = ths + [th_h], oms + [om_h]
+    t1, dt = 2.0, 0.25  # about 310 steps for the outlier network, at most 28 for the others
+    with native.MultiNetworks(ns, ks, seeds, cs, t1, dt, cluster_size=1, block_threads=256) as m:
+        order, _, acc = m.integrate(oms, ths, want_theta=False)
+        st = m.stats()
+        order2, _, _ = m.integrate(oms, ths, want_theta=False)
+    assert st["heavy"] >= 1
+    assert np.array_equal(order.view(np.uint32), order2.view(np.uint32))
+    h = len(ns) - 1
+    assert acc[h] > 10 * np.median(acc[:h])
+    with native.MultiNetworks([3000], [5], [77], [4.0], t1, dt, cluster_size=1, block_threads=256) as m:
+        alone, _, acc1 = m.integrate([om_h], [th_h], want_theta=False)
+        assert m.stats()["heavy"] == 0
+    assert np.max(np.abs(order[h] - alone[0])) < 2e-5
+    assert abs(int(acc[h]) - int(acc1[0])) <= 2
+    ref, tol = oracle_envelope(oracle_lib, th_h, om_h, 5, 4.0, 77, t1, dt)
+    assert np.all(np.abs(order[h] - ref.order) <= tol)
