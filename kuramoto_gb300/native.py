@@ -264,8 +264,16 @@ class Network:
             keep.append(f)
         _check(lib().kura_run(self.h, ctypes.byref(cb) if keep else None))
 
-    def state(self, traj=0):
-        th = np.zeros(self.n, np.float32)
+    def state(self, traj=0, out=None):
+        """(theta, t, h) of a trajectory; theta is written into ``out`` when given (a
+        contiguous float32 array of n values, e.g. in pinned memory)."""
+        if out is None:
+            th = np.zeros(self.n, np.float32)
+        else:
+            if not (isinstance(out, np.ndarray) and out.dtype == np.float32 and out.size == self.n
+                    and out.flags["C_CONTIGUOUS"] and out.flags["WRITEABLE"]):
+                raise ValueError("out must be a writeable contiguous float32 array of %d values" % self.n)
+            th = out
         t = ctypes.c_double()
         h = ctypes.c_double()
         _check(lib().kura_get_state(self.h, traj, _fptr(th), ctypes.byref(t), ctypes.byref(h)))

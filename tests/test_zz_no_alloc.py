@@ -48,6 +48,10 @@ def test_noalloc_matches_handle_api_twice(native):
     ref_r = [net.order(b) for b in range(B)]
     ref_th = [net.state(b)[0] for b in range(B)]
     ref_acc = net.stats()["accepted"]
+    # the final phases read into a caller's pinned buffer are the same values
+    buf = torch.empty(n, dtype=torch.float32).pin_memory().numpy()
+    got = net.state(B - 1, out=buf)[0]
+    assert got is buf and np.array_equal(buf, ref_th[B - 1])
     net.close()
 
     f = _entry(native)
