@@ -44,6 +44,7 @@ constexpr int M_RX = 2 * M_KMAX;      // slot of sum cos (sum sin follows)
 constexpr int M_ROW_BYTES = 9;        // shared memory per row: (cos, sin) + factor bits
 constexpr int M_SMEM_CAP = 200 * 1024;
 constexpr int M_MAX_CLUSTER = 16;
+constexpr int MU = 2;  // rows per thread whose loads are issued together in the row loop
 
 struct MInst {
   int n, k, seed, id;  // id: index of the network in the caller's order
@@ -211,40 +212,69 @@ struct Multi {
     for (int v = 0; v < M_NV; ++v) acc[v] = 0.f;
     const long long T = p.total;
     const bool proj = gout >= 0;
-    for (int i = r0 + tid; i < r1; i += NT) {
-      const long long gi = off + i;
-      const float om = p.omega[gi];
-      float gsum = 0.f;
-      for (int j = 0; j < nW; ++j) gsum = __fmaf_rn(S.Wst[si][j], p.g[(long long)slot_of(j, g1) * T + gi], gsum);
-      const f2 pr = two_prod(om, S.mhs[si]);
-      const f2 s1 = two_sum(p.ph_hi[base * T + gi], pr.hi);
-      const f2 s2 = two_sum(s1.hi, gsum);
-      const float lo = p.ph_lo[base * T + gi] + ((s1.lo + s2.lo) + __fmaf_rn(om, S.mls[si], pr.lo));
-      float sn, cs;
-      sincos_pair(s2.hi, lo, &sn, &cs);
-      xs[i - r0] = make_float2(cs, sn);
-      if (store_y7) {
-        const f2 y = two_sum(s2.hi, lo);
-        float hi7 = y.hi, lo7 = y.lo;
-        long long w7 = p.ph_w[base * T + gi];
-        wrap_phase(hi7, lo7, w7);
-        p.ph_hi[(base ^ 1) * T + gi] = hi7;
-        p.ph_lo[(base ^ 1) * T + gi] = lo7;
-        p.ph_w[(base ^ 1) * T + gi] = w7;
+    // MU rows per thread and pass: every load of the MU rows is issued before any of their
+    // arithmetic, so that their L2 latencies overlap (the shared-memory and y7 stores of a row
+    // keep the compiler from hoisting the next row's loads itself).  Only the r sums are
+    // accumulated here; the projections follow in a second pass over the rows' (cos, sin)
+    // in shared memory, which keeps the registers of this loop free for the batch.  Each
+    // thread visits its rows in the same order in both passes.
+    float Wr[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) Wr[j] = S.Wst[si][j];
+    const float mh = S.mhs[si], ml = S.mls[si];
+    for (int i0 = r0 + tid; i0 < r1; i0 += MU * NT) {
+      float om[MU], yh[MU], yl[MU], gs[MU];
+#pragma unroll
+      for (int q = 0; q < MU; ++q) {
+        const int i = i0 + q * NT;
+        const bool ok = i < r1;
+        const long long gi = off + i;
+        om[q] = ok ? p.omega[gi] : 0.f;
+        yh[q] = ok ? p.ph_hi[base * T + gi] : 0.f;
+        yl[q] = ok ? p.ph_lo[base * T + gi] : 0.f;
+        gs[q] = 0.f;
+#pragma unroll
+        for (int j = 0; j < 7; ++j)
+          if (j < nW) gs[q] = __fmaf_rn(Wr[j], ok ? p.g[(long long)slot_of(j, g1) * T + gi] : 0.f, gs[q]);
       }
-      if (proj) {
-        // sum over the rows with u_mn = +1 (the factor bits above k are zero)
+#pragma unroll
+      for (int q = 0; q < MU; ++q) {
+        const int i = i0 + q * NT;
+        if (i >= r1) break;
+        const long long gi = off + i;
+        const f2 pr = two_prod(om[q], mh);
+        const f2 s1 = two_sum(yh[q], pr.hi);
+        const f2 s2 = two_sum(s1.hi, gs[q]);
+        const float lo = yl[q] + ((s1.lo + s2.lo) + __fmaf_rn(om[q], ml, pr.lo));
+        float sn, cs;
+        sincos_pair(s2.hi, lo, &sn, &cs);
+        xs[i - r0] = make_float2(cs, sn);
+        if (store_y7) {
+          const f2 y = two_sum(s2.hi, lo);
+          float hi7 = y.hi, lo7 = y.lo;
+          long long w7 = p.ph_w[base * T + gi];
+          wrap_phase(hi7, lo7, w7);
+          p.ph_hi[(base ^ 1) * T + gi] = hi7;
+          p.ph_lo[(base ^ 1) * T + gi] = lo7;
+          p.ph_w[(base ^ 1) * T + gi] = w7;
+        }
+        acc[M_RX] += cs;
+        acc[M_RX + 1] += sn;
+      }
+    }
+    if (proj) {
+      // sum over the rows with u_mn = +1 (the factor bits above k are zero)
+      for (int i = r0 + tid; i < r1; i += NT) {
+        const float2 x = xs[i - r0];
         const uint32_t u = ubits[i - r0];
 #pragma unroll
         for (int m = 0; m < M_KMAX; ++m) {
           if (u & (1u << m)) {
-            acc[2 * m] += cs;
-            acc[2 * m + 1] += sn;
+            acc[2 * m] += x.x;
+            acc[2 * m + 1] += x.y;
           }
         }
       }
-      acc[M_RX] += cs;
-      acc[M_RX + 1] += sn;
     }
     // sum_n u_mn x_n = 2 (sum over u_mn = +1) - sum_n x_n
     if (proj) {
