@@ -185,3 +185,28 @@ def test_heavy_network_runs_beside_the_main_launch(native, oracle_lib):
     assert abs(int(acc[h]) - int(acc1[0])) <= 2
     ref, tol = oracle_envelope(oracle_lib, th_h, om_h, 5, 4.0, 77, t1, dt)
     assert np.all(np.abs(order[h] - ref.order) <= tol)
+
+
+@pytest.mark.parametrize("shape", [(1, 256), (16, 256)])
+def test_tiny_networks_and_empty_ctas(native, oracle_lib, shape):
+    """Networks smaller than the cluster leave CTAs without rows (n = 1 in a 16-CTA cluster);
+    ragged sizes around a warp (31, 33) and K = 0 (uncoupled) ride along.  Every network
+    matches its FP64 oracle run."""
+    ns = np.array([1, 2, 31, 33, 64, 5], np.int64)
+    ks = np.array([1, 2, 5, 8, 3, 0])
+    seeds = np.array([3, 5, 7, 11, 13, 17])
+    cs = np.float32([2.0, 5.0, 3.0, 4.5, 1.0, 3.0])
+    ths, oms = [], []
+    for i, n in enumerate(ns):
+        th, om = normal_inputs(int(n), 900 + i, init=2 * np.pi)
+        ths.append(th)
+        oms.append(om)
+    t1, dt = 4.0, 0.5
+    with native.MultiNetworks(ns, ks, seeds, cs, t1, dt, cluster_size=shape[0], block_threads=shape[1]) as m:
+        order, thetas, acc = m.integrate(oms, ths)
+    for i in range(len(ns)):
+        ref, tol = oracle_envelope(oracle_lib, ths[i], oms[i], ks[i], cs[i], seeds[i], t1, dt)
+        assert order[i].size == ref.order.size
+        assert np.all(np.abs(order[i] - ref.order) <= tol), i
+        assert abs(int(acc[i]) - ref.steps) <= max(2, ref.steps // 50), (i, acc[i], ref.steps)
+        assert thetas[i].size == ns[i]
