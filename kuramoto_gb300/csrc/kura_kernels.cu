@@ -66,6 +66,17 @@ __device__ __forceinline__ uint4 ld_stream_u4(const int8_t* p) {
 __device__ __forceinline__ float i8_to_f(uint32_t w_biased, int j) {
   return __int_as_float((int)__byte_perm(w_biased, 0x4B000000u, 0x7540u + (unsigned)j)) - 8388736.0f;
 }
+// 16 bytes global -> shared without a register round trip (L2 only); src_bytes 0 zero-fills
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, int src_bytes) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(gsrc), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ float4 ld_stream4(const float* p) {
   float4 v;
   asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
@@ -113,7 +124,9 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[7] = o; o += align16(coup != KURA_COUPLING_VOLCANO ? bmax * (bmax == 1 ? (coup == COUP_DENSE_I8 ? CT_I8 : CT_F1) : CT) * 8 : 0); // x tile
   // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
   off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
-  off[9] = o; o += align16(coup == KURA_COUPLING_VOLCANO && xs_smem ? bmax * rows * 8 : 0);  // own (cos, sin)
+  // own (cos, sin) (volcano); the ring of A chunks in flight (dense float)
+  off[9] = o; o += align16(coup == KURA_COUPLING_VOLCANO && xs_smem ? bmax * rows * 8
+                           : (coup == KURA_COUPLING_DENSE ? KW * A_STAGES * A_ROWS * 32 * 16 : 0));
   *total = o;
 }
 
@@ -159,7 +172,7 @@ template <int COUP, int BMAX, int KMAX>
 struct Engine {
   static constexpr int PW = pw_of(COUP, KMAX);
   // rows per warp and pass of the dense coupling: each staged x value is reused RG times
-  static constexpr int RG = BMAX == 1 ? 4 : (BMAX == 2 ? 4 : 4);
+  static constexpr int RG = A_ROWS;
 
   const KParams& p;
   TrajG* tr;
@@ -173,6 +186,7 @@ struct Engine {
   float2* xt;
   float* f3;
   float2* xs;   // (cos, sin) of the CTA's rows, [b][rows]: shared memory, or the CTA's part of xbuf
+  float4* ring;  // [warp][A_STAGES][A_ROWS][lane] (dense float coupling)
   int G, gi, tid, lane, warp, r0, r1, B;
   unsigned target;
   int nbar, xpar;
@@ -202,6 +216,7 @@ struct Engine {
     nbar = 0;
     xpar = 0;
     xs = pp.xs_smem ? (float2*)(smem + off[9]) : nullptr;
+    ring = (float4*)(smem + off[9]);  // the dense float product's chunks of A in flight
   }
 
   // (cos, sin) of row i of trajectory b for the volcano coupling (own rows only)
@@ -745,12 +760,17 @@ struct Engine {
   }
 
   // A (rows r0..r1 of this CTA) times the (cos, sin) of every trajectory.  x is
-  // staged in shared memory one column tile at a time; each warp keeps RG rows in
-  // flight, each lane reading 16-byte chunks of them.
+  // staged in shared memory one column tile at a time; each warp works on RG rows, each
+  // lane on 16-byte chunks of them, A_STAGES chunks per row in flight.
   static constexpr int CTF = BMAX == 1 ? CT_F1 : CT;  // columns per x tile of the float product
   __device__ void dense_matvec() {
     const int ld = p.ld;
     const int rows_per_pass = KW * RG;
+    // A streams through a per-warp ring in shared memory with cp.async: every lane copies its
+    // own 16 bytes of each of the warp's RG rows, A_STAGES column steps ahead, and reads back
+    // only what it copied, so the ring needs no barrier and holds no registers per byte in
+    // flight.  Rows past the CTA's block are zero-filled.
+    float4* my = ring + (size_t)warp * (A_STAGES * RG * 32) + lane;
     for (int pr0 = r0; pr0 < r1; pr0 += rows_per_pass) {
       float acc[RG][BMAX][2];
 #pragma unroll
@@ -759,6 +779,14 @@ struct Engine {
         for (int b = 0; b < BMAX; ++b) acc[q][b][0] = acc[q][b][1] = 0.f;
       // warp w takes rows pr0 + w + KW*q of the pass, so small row blocks keep every warp busy
       const int row0 = pr0 + warp;
+      const float* src[RG];
+      int nb[RG];
+#pragma unroll
+      for (int q = 0; q < RG; ++q) {
+        const int row = row0 + KW * q;
+        nb[q] = row < r1 ? 16 : 0;
+        src[q] = p.adj + (size_t)(row < r1 ? row : r0) * ld + lane * 4;
+      }
       for (int c0 = 0; c0 < ld; c0 += CTF) {
         __syncthreads();
         const int cw = min(CTF, ld - c0);
@@ -767,13 +795,29 @@ struct Engine {
           xt[b * CTF + c] = (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
         }
         __syncthreads();
-        for (int cc = lane * 4; cc < cw; cc += 128) {
+        // column steps of this lane: cc = lane*4 + 128*it < cw (cw is a multiple of 32)
+        const int nit = (cw - lane * 4 + 127) >> 7;
+#pragma unroll
+        for (int s = 0; s < A_STAGES - 1; ++s) {
+          if (s < nit)
+#pragma unroll
+            for (int q = 0; q < RG; ++q) cp_async16(my + (s * RG + q) * 32, src[q] + c0 + 128 * s, nb[q]);
+          cp_async_commit();
+        }
+        for (int it = 0; it < nit; ++it) {
+          const int ahead = it + A_STAGES - 1;
+          if (ahead < nit) {
+            const int sl = ahead % A_STAGES;
+#pragma unroll
+            for (int q = 0; q < RG; ++q) cp_async16(my + (sl * RG + q) * 32, src[q] + c0 + 128 * ahead, nb[q]);
+          }
+          cp_async_commit();
+          cp_async_wait<A_STAGES - 1>();  // the chunks of step it have landed
+          const int sl = it % A_STAGES;
           float4 a[RG];
 #pragma unroll
-          for (int q = 0; q < RG; ++q) {
-            int row = row0 + KW * q;
-            a[q] = (row < r1) ? ld_stream4(p.adj + (size_t)row * ld + c0 + cc) : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
+          for (int q = 0; q < RG; ++q) a[q] = my[(sl * RG + q) * 32];
+          const int cc = lane * 4 + 128 * it;
 #pragma unroll
           for (int b = 0; b < BMAX; ++b) {
             if (b < B) {
@@ -787,6 +831,7 @@ struct Engine {
             }
           }
         }
+        cp_async_wait<0>();
       }
 #pragma unroll
       for (int q = 0; q < RG; ++q)
