@@ -9,7 +9,7 @@
 // For the reference's volcano rule N*A_ij is an integer in [-K, K], exact in BF16, so the
 // product carries the precision of the hi+lo split of X (about 2^-16).  A general
 // adjacency is split as N A = A_hi + A_lo and the term A_lo X_hi comes from a second GEMM
-// pass (spec: split-BF16 hi+lo, FP32 accumulation).
+// pass (split-BF16 hi + lo operands, FP32 accumulation).
 //
 // The DP45 attempt (dp45_step, dp45.cu:87-141) is a fixed sequence of launches --
 // coefficients, 6 x (stage, GEMM), error norm, controller, outputs -- captured once in a

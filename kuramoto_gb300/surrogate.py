@@ -12,7 +12,7 @@ The pipeline:
 3. For a sweep over c, short runs of the candidate couplings (t <= 9) give the features. The
    network predicts the steady statistics, and the sweep points go where the predicted
    statistics change fastest.
-4. Every placed point is then integrated to t1 by the DP45 solver. The solver judges each
+4. Every placed point is then integrated to t1 by the DP45 solver. The solver checks each
    prediction (tolerance 0.02 in r), and its values replace the predictions that miss.
 
 The reference has no counterpart; it integrates one network per process and leaves

@@ -2,7 +2,7 @@
 
 Training data come from the batched multi-network solver. The MLP is trained by the
 library's kernels. A sweep over c for one network places 64 points where the predicted
-steady statistics of r change fastest, and the DP45 solver integrates every point and judges
+steady statistics of r change fastest, and the DP45 solver integrates every point and checks
 each prediction.  A dense DP45 sweep of the same network locates the true transition, and
 the test measures what the network gains over the method without it (64 evenly spaced
 points): how many points land in the transition window, and what an even sweep would cost to
@@ -43,7 +43,7 @@ def test_sweep_placement_beats_even_spacing(trained):
     S, sur, _, _, _ = trained
     k, f, seed = 5, 1.0, 77
     res = S.sweep(sur, N, k, f, 0, seed, np.random.default_rng(3), npoints=64, candidates=64, t1=T1)
-    # every prediction judged by DP45; the tolerance of the sweep is 0.02 in r
+    # every prediction checked by DP45; the tolerance of the sweep is 0.02 in r
     assert res["within_tol"].mean() >= 0.95
     assert np.all(np.isfinite(res["value"]))
     # the true transition from a dense DP45 sweep of the same network
