@@ -627,7 +627,7 @@ struct kura_multi {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t evf = nullptr, evj = nullptr;  // fork after the pilot, join of the heavy launch
   MInst* d_instH = nullptr;
-  int heavy = 0, heavy_cs = 0;
+  int heavy = 0;
   MInst* d_inst = nullptr;
   int *d_queue = nullptr, *d_status = nullptr;
   float *d_om = nullptr, *d_th = nullptr, *d_hi = nullptr, *d_lo = nullptr, *d_g = nullptr, *d_r = nullptr,
@@ -1004,7 +1004,6 @@ extern "C" int kura_multi_integrate(kura_multi* m, const float* omega, const flo
     }
   }
   m->heavy = nh;
-  m->heavy_cs = hcs;
   MCU(cudaMemcpyAsync(m->d_inst2, order2.data() + nh, sizeof(MInst) * (m->count - nh), cudaMemcpyHostToDevice,
                       m->st));
   {
