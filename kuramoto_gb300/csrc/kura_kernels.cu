@@ -121,7 +121,10 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[4] = o; o += align16(sl * 4);                      // slice
   off[5] = o; o += align16(16 * 4);                      // flags
   off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
-  off[7] = o; o += align16(coup != KURA_COUPLING_VOLCANO ? bmax * (bmax == 1 ? (coup == COUP_DENSE_I8 ? CT_I8 : CT_F1) : CT) * 8 : 0); // x tile
+  // x tile; the int8 product's has 2 (cos, sin) pairs of padding per 16 columns
+  off[7] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? 0
+                           : coup == COUP_DENSE_I8 ? bmax * ((bmax == 1 ? CT_I8 : CT) / 16) * I8_CHUNK * 8
+                                                   : bmax * (bmax == 1 ? CT_F1 : CT) * 8);
   // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
   off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
   // own (cos, sin) (volcano); the ring of A chunks in flight (dense float)
@@ -855,6 +858,10 @@ struct Engine {
   }
 
   static constexpr int CTX = BMAX == 1 ? CT_I8 : CT;  // columns per x tile of the int8 product
+  // Each lane's 16 columns of x are 128 bytes apart from the next lane's.  Stored back to
+  // back, all 32 lanes would read the same four banks; a stride of I8_CHUNK = 18 (cos, sin)
+  // pairs (144 bytes) per 16 columns spreads them over eight 16-byte bank groups.
+  static constexpr int CTXP = CTX / 16 * I8_CHUNK;
   // one pass over RG rows per warp (rows pr0 + warp + KW*q), CPL int8 columns per lane and load
   template <int RG, int CPL>
   __device__ void mv_i8_pass(int pr0) {
@@ -871,7 +878,8 @@ struct Engine {
       const int cw = min(CTX, ld8 - c0);  // a multiple of 16
       for (int t = tid; t < B * CTX; t += KT) {
         int b = t / CTX, c = t - b * CTX;
-        xt[b * CTX + c] = (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
+        xt[b * CTXP + (c >> 4) * I8_CHUNK + (c & 15)] =
+            (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
       }
       __syncthreads();
       for (int cc = lane * CPL; cc < cw; cc += 32 * CPL) {
@@ -899,7 +907,7 @@ struct Engine {
 #pragma unroll
           for (int b = 0; b < BMAX; ++b) {
             if (b < B) {
-              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTX + cc + 4 * wd);
+              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTXP + (cc >> 4) * I8_CHUNK + 4 * wd);
               const float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
 #pragma unroll
               for (int q = 0; q < RG; ++q) {
