@@ -124,7 +124,7 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   // x tile; the int8 product's has 2 (cos, sin) pairs of padding per 16 columns
   off[7] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? 0
                            : coup == COUP_DENSE_I8 ? bmax * ((bmax == 1 ? CT_I8 : CT) / 16) * I8_CHUNK * 8
-                                                   : bmax * (bmax == 1 ? CT_F1 : CT) * 8);
+                                                   : bmax * ((bmax == 1 ? CT_F1 : CT) / 4) * F_CHUNK * 8);
   // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
   off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
   // own (cos, sin) (volcano); the ring of A chunks in flight (dense float)
@@ -766,6 +766,10 @@ struct Engine {
   // staged in shared memory one column tile at a time; each warp works on RG rows, each
   // lane on 16-byte chunks of them, A_STAGES chunks per row in flight.
   static constexpr int CTF = BMAX == 1 ? CT_F1 : CT;  // columns per x tile of the float product
+  // A lane's 4 columns of x are 32 bytes from the next lane's, so back to back they would
+  // fall on four of the eight 16-byte bank groups; a stride of F_CHUNK = 6 (cos, sin) pairs
+  // (48 bytes) per 4 columns uses all eight.
+  static constexpr int CTFP = CTF / 4 * F_CHUNK;
   __device__ void dense_matvec() {
     const int ld = p.ld;
     const int rows_per_pass = KW * RG;
@@ -795,7 +799,8 @@ struct Engine {
         const int cw = min(CTF, ld - c0);
         for (int t = tid; t < B * CTF; t += KT) {
           int b = t / CTF, c = t - b * CTF;
-          xt[b * CTF + c] = (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
+          xt[b * CTFP + (c >> 2) * F_CHUNK + (c & 3)] =
+              (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
         }
         __syncthreads();
         // column steps of this lane: cc = lane*4 + 128*it < cw (cw is a multiple of 32)
@@ -824,7 +829,7 @@ struct Engine {
 #pragma unroll
           for (int b = 0; b < BMAX; ++b) {
             if (b < B) {
-              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTF + cc);
+              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTFP + (cc >> 2) * F_CHUNK);
               float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
 #pragma unroll
               for (int q = 0; q < RG; ++q) {

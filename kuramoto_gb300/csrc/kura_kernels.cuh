@@ -14,6 +14,7 @@ constexpr int CT_F1 = 4096;   // the same for float rows and one trajectory
 constexpr int A_ROWS = 4;     // rows per warp and pass of the dense float product
 constexpr int A_STAGES = 3;   // 16-byte chunks per row and lane in flight (cp.async ring) in that product
 constexpr int I8_CHUNK = 18;  // x tile stride of the int8 product per 16 columns, in (cos, sin) pairs
+constexpr int F_CHUNK = 6;    // the same for the float product per 4 columns
 constexpr int PW_MAX = 2 * 32 + 2;  // partial sums per trajectory and CTA: 2K projections + (sum cos, sum sin)
 
 // Per-trajectory scalars.  Every CTA keeps an identical copy in shared memory
