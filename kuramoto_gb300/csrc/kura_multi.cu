@@ -3,8 +3,8 @@
 // Each network (its own N, rank K <= 8, coupling c, Philox seed, frequencies and initial
 // phases) is integrated from t = 0 to t1 with its own adaptive DP45 step (dp45_run,
 // dp45.cu:148-164; the reference runs one `kuramoto -A` process per network) by one
-// thread-block cluster.  Clusters pull networks from a work queue ordered largest first,
-// so nothing synchronises the grid: a network's reductions (the K-mode projections of the
+// thread-block cluster.  Clusters pull networks from a work queue (largest first in the
+// pilot launch, then by predicted remaining work), so nothing synchronises the grid: a network's reductions (the K-mode projections of the
 // regenerated volcano coupling, kuramoto.cu:62-101, the error norm, dp45.cu:116-119, and
 // the order parameter, kuramoto.cu:587-600) go through distributed shared memory between
 // the CTAs of its cluster, with hardware cluster barriers.  The factor bits of a CTA's rows
@@ -17,10 +17,11 @@
 // cluster on bitwise identical sums, so all CTAs take the same decisions without
 // exchanging them, and every cluster barrier is reached by all of them.
 //
-// The launch shape (cluster size, block size) comes from an autotuner that times a
-// stratified sample of the networks at every candidate shape.  An integration is a pilot
-// launch (a CUDA graph replayed every time) followed by the rest of the work in the order
-// of predicted cost, the heaviest networks in large clusters beside the others.
+// The launch shape (cluster size, block size) comes from an autotuner that runs a
+// stratified sample of the networks at every candidate shape and predicts the time of the
+// whole integration from it.  An integration is a pilot launch (a CUDA graph replayed every
+// time) followed by the rest of the work in the order of predicted cost, the heaviest
+// networks in large clusters beside the others.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <algorithm>
