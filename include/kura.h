@@ -201,7 +201,10 @@ typedef struct kura_multi kura_multi;
  * 4 bytes per record).  Records: r at t = 0 and at dt*m, m = 1 .. int(t1/dt) in float,
  * as the reference's order.dat (kuramoto.cu:543-626).  h0 is the first trial step of every
  * network.  cluster_size (1, 2, 4, 8, 16) and block_threads (256, 512, 1024) fix the launch
- * shape; 0 lets the autotuner choose it at the first integration. */
+ * shape; 0 lets the autotuner choose it at the first integration, as the shape with the
+ * shortest predicted time for the whole integration (environment KURA_MULTI_TUNE_LOG=1
+ * prints its trials).  Later integrations on the handle keep the shape and give bitwise
+ * identical results for the same inputs. */
 int kura_multi_create(const kura_instance* inst, int32_t count, double t1, double dt, double h0, double atol,
                       double rtol, int32_t device, int32_t cluster_size, int32_t block_threads, kura_multi** out);
 void kura_multi_destroy(kura_multi* m);
