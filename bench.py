@@ -234,9 +234,6 @@ def run_native(args, w):
     e2e_ms = 0.0
     h2d = d2h = 0
 
-    def pinned(a):
-        return torch.from_numpy(np.ascontiguousarray(a, np.float32)).pin_memory().numpy()
-
     om_pin = pinned(om)
     th_pin = [pinned(t) for t in thetas]
     fin_pin = [pinned(np.zeros(n, np.float32)) for _ in range(B)]
@@ -327,6 +324,12 @@ def multi_inputs(w, seed):
     return ns, ks, seeds, cs, ths, oms
 
 
+def pinned(a):
+    """A float32 copy of `a` in pinned host memory (a numpy view of a pinned torch tensor)."""
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).pin_memory().numpy()
+
+
 def run_multi(args, w):
     import torch
     import kuramoto_gb300 as kg
@@ -338,8 +341,8 @@ def run_multi(args, w):
         dist.init_process_group("nccl")
     nets = multi_inputs(w, instance_seed(rank))
     ns, ks, seeds, cs, ths, oms = nets
-    om = np.concatenate(oms)
-    th = np.concatenate(ths)
+    om = pinned(np.concatenate(oms))  # the e2e leg copies them in from pinned memory
+    th = pinned(np.concatenate(ths))
     m = kg.MultiNetworks(ns, ks, seeds, cs, w["t1"], w["dt"], atol=w["atol"], rtol=w["rtol"], device=local)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
 
