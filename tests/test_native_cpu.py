@@ -74,6 +74,19 @@ def test_invalid_config_rejected_without_gpu(native):
         assert e.value.code == code
 
 
+def test_invalid_mlp_rejected_without_gpu(native):
+    """Surrogate shapes outside what the tensor-core kernels support fail before any device
+    work: input or output width 0 or above 64, a hidden width other than 64/128/256, a batch
+    that is not a multiple of 128 in 128..4096."""
+    for kw in (dict(in_dim=0), dict(in_dim=65), dict(out_dim=0), dict(out_dim=65), dict(hidden=100),
+               dict(batch=100), dict(batch=8192)):
+        args = dict(in_dim=14, out_dim=2, hidden=256, batch=512)
+        args.update(kw)
+        with pytest.raises(native.KuraError) as e:
+            native.MLP(**args)
+        assert e.value.code == -7
+
+
 def test_cli_help_runs_without_gpu(native):
     r = subprocess.run([native.cli_path(), "-h"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "usage:" in r.stdout and "filebase" in r.stdout
