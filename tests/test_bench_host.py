@@ -1,0 +1,65 @@
+"""bench.py's host arithmetic on the CPU: the seeded multi-network workload and the roofline
+fields of the JSON line (algorithmic bytes or flops per unit over the kernel time)."""
+import json
+import os
+import types
+
+import numpy as np
+
+import bench
+
+
+def test_multi_inputs_are_seeded_and_in_range():
+    w = bench.WORKLOADS["multi512"]
+    a = bench.multi_inputs(w, bench.instance_seed(0))
+    b = bench.multi_inputs(w, bench.instance_seed(0))
+    ns, ks, seeds, cs, ths, oms = a
+    assert len(ns) == 512 and int(ns.sum()) == 3135408
+    assert ns.min() >= 1000 and ns.max() <= 20000
+    assert ks.min() >= 2 and ks.max() <= 8 and cs.min() >= 0.0 and cs.max() <= 6.0
+    assert all(t.size == n and o.size == n for t, o, n in zip(ths, oms, ns))
+    assert all(np.array_equal(x, y) for x, y in zip(a[4] + a[5], b[4] + b[5]))
+    other = bench.multi_inputs(w, bench.instance_seed(1))  # another rank's instance
+    assert not np.array_equal(other[0], ns)
+
+
+def _args(workload, steps):
+    return types.SimpleNamespace(workload=workload, steps=steps)
+
+
+def test_dense_roofline_counts_a_once_per_rhs():
+    w = bench.WORKLOADS["dense65536"]
+    n = w["n"]
+    res = dict(kernel_ms=90.0, launches=1, acc_per_step=6)
+    r = bench.roofline(w, res, _args("dense65536", 1))
+    expect = 24.0 * n * 6 * n / 0.090 / 1e9  # 6 RHS x 4N^2 bytes per accepted step
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s"
+    assert abs(r["achieved"] - round(expect, 1)) < 0.11
+    assert abs(r["frac"] - round(r["achieved"] / r["peak"], 4)) < 1e-4
+    prof = json.load(open(os.path.join(bench.ROOT, "profiles", "traffic.json")))["dense65536"]
+    assert abs(r["traffic"] - prof["bytes_per_accepted_osc_step"] * 6 * n) < 1.0
+
+
+def test_int8_roofline_counts_one_byte_per_entry():
+    w = bench.WORKLOADS["dense65536i8"]
+    n = w["n"]
+    r = bench.roofline(w, dict(kernel_ms=39.0, launches=1, acc_per_step=6), _args("dense65536i8", 1))
+    assert abs(r["bytes_per_unit"] - 6.0 * n) < 1e-6
+
+
+def test_tensor_roofline_counts_algorithmic_flops():
+    w = bench.WORKLOADS["ensemble65536"]
+    n = w["n"]
+    acc = 700  # accepted steps summed over the batch, one integration
+    r = bench.roofline(w, dict(kernel_ms=2 * 114.5, launches=8, acc_per_step=acc), _args("ensemble65536", 2))
+    expect = 24.0 * n * acc * n / 0.1145 / 1e12
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+    assert abs(r["achieved"] - round(expect, 2)) < 0.011
+    assert r["issued_flops_per_unit"] == 2 * r["flops_per_unit"] == 48.0 * n
+
+
+def test_volcano_roofline_uses_the_state_bytes():
+    w = bench.WORKLOADS["volcano200k"]
+    r = bench.roofline(w, dict(kernel_ms=39.9, launches=1, acc_per_step=1023), _args("volcano200k", 1))
+    assert r["bytes_per_unit"] == bench.STATE_BYTES == 150.0
+    assert abs(r["achieved"] - round(150.0 * 1023 * w["n"] / 0.0399 / 1e9, 1)) < 0.11
