@@ -629,8 +629,8 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": value, "unit": "osc-steps/s", "cores": threads, "kind": "port",
-                                 "sample": "whole workload per step (5 trajectories to t=%g), float32 oracle "
-                                           "restating the reference program, OpenMP" % w["t1"]},
+                                 "sample": "whole workload per step (%d trajectories to t=%g), float32 oracle "
+                                           "restating the reference program, OpenMP" % (B, w["t1"])},
                 "e2e": {"value": value, "unit": "osc-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -651,8 +651,8 @@ def main():
     if not args.no_cpu:
         v, el, steps = cpu_baseline(w, res["om"], res["thetas"], threads)
         line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
-                                "sample": "whole workload (5 trajectories to t=%g, %d accepted steps, %.1f s), "
-                                          "float32 oracle restating the reference program" % (w["t1"], steps, el)}
+                                "sample": "whole workload (%d trajectories to t=%g, %d accepted steps, %.1f s), "
+                                          "float32 oracle restating the reference program" % (B, w["t1"], steps, el)}
         ci = len(w["cs"]) // 2
         line["r_err_vs_fp64"] = r_error_vs_fp64(w, res["om"], res["thetas"][ci], w["cs"][ci], res["orders"][ci],
                                                 threads)
