@@ -51,9 +51,14 @@ WORKLOADS = {
     "dense65536i8": dict(n=65536, k=5, coupling=0, cs=[3.0], normal=False, init=2 * np.pi, t1=0.004, dt=0.001,
                          atol=1e-6, rtol=0.0, shared_theta=False, adj_storage=1),
     # the shared-adjacency ensemble on tensor cores: N=65536, K=5 dense volcano adjacency,
-    # 128 trajectories with distinct theta0 uniform in [0, 2pi), shared Cauchy omega, c=3
-    "ensemble65536": dict(n=65536, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
-                          dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False, engine="tensor"),
+    # 128 trajectories with distinct theta0 uniform in [0, 2pi), shared Cauchy omega, c=3,
+    # integrated toward t=20 with records every 0.01; one bench step is a window of 0.05 time
+    # units that continues the same integration (warm-up windows start it from t=0).  The
+    # plain FP32 path (`dense65536w`) runs trajectory 0 of the same inputs beside it.
+    "ensemble65536": dict(kind="windows", n=65536, k=5, cs=[3.0] * 128, init=2 * np.pi, t1=20.0, dt=0.01,
+                          window=0.05, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
+    "dense65536w": dict(kind="windows", n=65536, k=5, cs=[3.0], init=2 * np.pi, t1=20.0, dt=0.01, window=0.05,
+                        atol=1e-6, rtol=0.0, engine="persistent"),
     # the same ensemble at N=16384 (a 512 MiB BF16 adjacency, still larger than L2): profiling captures
     "ensemble16384": dict(n=16384, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
                           dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False, engine="tensor"),
@@ -581,13 +586,293 @@ def r_error_vs_fp64(w, om, theta, c, gpu_order, threads, t1=3.0):
     return float(np.max(np.abs(r.order[:m] - gpu_order[:m])))
 
 
+# ------------------------------------------------------------------ windowed workloads
+def window_inputs(w, seed, host_rng):
+    """Shared Cauchy omega (glibc rand of `seed`, scale 1, the reference's generator) and one
+    theta0 per trajectory, uniform in [0, init), from a numpy stream of `seed`.  Trajectory 0 is
+    the same for every batch size, so the plain path integrates the ensemble's first member."""
+    n, B = w["n"], len(w["cs"])
+    _, om = host_rng(seed, n, 0.0, 1.0, False, gen_theta=False)
+    rng = np.random.default_rng(seed)
+    return [(rng.random(n) * w["init"]).astype(np.float32) for _ in range(B)], om
+
+
+class Windowed:
+    """One integration toward t1 on one handle, advanced a window at a time: kura_set_horizon
+    after a finished kura_run continues every trajectory on the device (phases, FSAL slope and
+    step size kept), so the windows are consecutive pieces of one uninterrupted run."""
+
+    def __init__(self, w, thetas, om, seed, device, stream):
+        import kuramoto_gb300 as kg
+        self.w = w
+        self.n, self.B = w["n"], len(thetas)
+        eng = kg.ENGINE_TENSOR if w["engine"] == "tensor" else kg.ENGINE_PERSISTENT
+        self.net = kg.Network(self.n, k=w["k"], coupling=kg.COUPLING_DENSE, batch=self.B, seed=seed, atol=w["atol"],
+                              rtol=w["rtol"], dense_level=0, device=device, stream=stream, engine=eng)
+        self.net.set_frequencies(om)
+        self.net.generate_adjacency()
+        for b in range(self.B):
+            self.net.set_coupling(b, w["cs"][b])
+            self.net.set_state(b, thetas[b], 0.0, w["dt"] / 100)
+        self.t_end = 0.0
+        self.first = True
+        self.rec = [dict() for _ in range(self.B)]  # t_eval -> r
+
+    def horizon(self):
+        self.t_end += self.w["window"]
+        self.net.set_horizon(self.t_end, self.w["dt"], self.first)
+        self.first = False
+
+    def run(self):
+        rec = self.rec
+        self.net.run(on_output=lambda b, i, te, r, th, cp: rec[b].__setitem__(round(te, 9), r) and False)
+
+    def close(self):
+        self.net.close()
+
+
+def timed_windows(win, steps, stream, clocks=None):
+    """`steps` windows timed with CUDA events on the handle's stream; returns the accepted
+    oscillator-steps, the event time and the stats deltas."""
+    import torch
+    st0 = win.net.stats()
+    ms = 0.0
+    for _ in range(steps):
+        win.horizon()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        win.run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+    st1 = win.net.stats()
+    d = {k: st1[k] - st0[k] for k in ("accepted", "rejected", "launches", "kernel_ms", "coupling_ms",
+                                     "coupling_launches")}
+    return d["accepted"] * win.n, ms, d
+
+
+def fp64_records(w, theta0, om, c, t1, threads):
+    """r of one trajectory from the FP64 oracle (rank-K form: the same matrix as the stored
+    dense volcano adjacency, at O(N K) per RHS) at t = 0, dt, .., keyed like the GPU records."""
+    from oracle import kora
+    r = kora.run(theta0, om, k=w["k"], c1=c, onthefly=True, seed=1, fp64=True, t1=t1, dt=w["dt"], atol=w["atol"],
+                 rtol=w["rtol"], threads=threads)
+    keys = [round(float(np.float32(np.float32(w["dt"]) * np.float32(i))), 9) for i in range(r.order.size)]
+    keys[0] = 0.0
+    return dict(zip(keys, r.order)), r.steps
+
+
+def window_cpu(w, theta0, om, c, t1, threads):
+    """The float32 oracle port of the reference program on one trajectory from t = 0 to t1, the
+    coupling in its rank-K form (kuramoto.cu:62-101 arithmetic; the same matrix as the dense A)."""
+    from oracle import kora
+    t0 = time.perf_counter()
+    r = kora.run(theta0, om, k=w["k"], c1=c, onthefly=True, seed=1, fp64=False, t1=t1, dt=w["dt"], atol=w["atol"],
+                 rtol=w["rtol"], threads=threads)
+    el = time.perf_counter() - t0
+    return r.steps * w["n"] / el, el, r.steps
+
+
+CPU_WINDOWS = 4  # the CPU sample: one trajectory over this many windows from t = 0
+
+
+def main_windows(args, w):
+    ws, rank, local = dist_env()
+    n, B = w["n"], len(w["cs"])
+    threads = os.cpu_count() or 1
+    metric = "accepted DP45 steps x N x batch / s"
+    config = {"workload": args.workload, "n": n, "k": w["k"], "coupling": "dense volcano adjacency (seed 1)",
+              "engine": "tcgen05 split-BF16 ensemble" if w["engine"] == "tensor" else "plain FP32 persistent",
+              "batch": B, "c": w["cs"][0], "theta0": "uniform [0, 2pi), one numpy stream per seed",
+              "frequencies": "cauchy scale 1 (glibc rand, seed 1), shared", "t1": w["t1"], "dt": w["dt"],
+              "window": w["window"], "atol": w["atol"], "rtol": w["rtol"],
+              "step": "one window of %g time units continuing the same integration toward t1; warm-up windows "
+                      "start it from t=0" % w["window"],
+              "l2": "inputs larger than L2 (the adjacency, %.1f GB, is streamed by every RHS); not flushed"
+                    % (n * n * (2 if w["engine"] == "tensor" else 4) / 1e9),
+              "parallelism": "replicas" if ws > 1 else "single"}
+    sample = ("trajectory b = step mod %d from t=0 to t=%g (%d windows), float32 oracle restating the reference "
+              "program, coupling in its rank-K form, OpenMP" % (B, CPU_WINDOWS * w["window"], CPU_WINDOWS))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import kora
+        thetas, om = window_inputs(w, 1, kora.host_random_inputs)
+        for i in range(args.warmup):
+            window_cpu(w, thetas[i % B], om, w["cs"][i % B], w["window"], threads)
+        units = el = 0.0
+        for i in range(args.steps):
+            v, e, st = window_cpu(w, thetas[i % B], om, w["cs"][i % B], CPU_WINDOWS * w["window"], threads)
+            units += st * n
+            el += e
+        value = units / el
+        print(json.dumps({"impl": "reference", "metric": metric, "value": value, "unit": "osc-steps/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                          "cpu_baseline": {"value": value, "unit": "osc-steps/s", "cores": threads, "kind": "port",
+                                           "sample": sample},
+                          "e2e": {"value": value, "unit": "osc-steps/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    import kuramoto_gb300 as kg
+    os.environ.setdefault("KURA_TIME_COUPLING", "1")
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    seed = instance_seed(rank)
+    thetas, om = window_inputs(w, seed, kg.random_inputs)
+    stream = torch.cuda.current_stream()
+    win = Windowed(w, thetas, om, seed, local, stream.cuda_stream)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        win.horizon()
+        win.run()
+    barrier()
+    with Clocks(local) as clk:
+        units, ms, d = timed_windows(win, args.steps, stream)
+        barrier()
+    units_all, ms_max = combine_ranks(units, ms, "cuda")
+    value = units_all / (ms_max / 1e3)
+    t_value_end = win.t_end
+
+    # ---- e2e: the same windows through host buffers (frequencies and every trajectory's phases
+    # copied in from pinned memory with their own t and h; records and phases copied out)
+    om_pin = pinned(om)
+    th_pin = [pinned(np.zeros(n, np.float32)) for _ in range(B)]
+    th_t = [0.0] * B
+    th_h = [0.0] * B
+    for b in range(B):
+        _, th_t[b], th_h[b] = win.net.state(b, out=th_pin[b])
+    e2e_units = e2e_s = 0.0
+    h2d = d2h = 0
+    for it in range(args.steps):
+        barrier()
+        t0 = time.perf_counter()
+        win.net.set_frequencies(om_pin)
+        for b in range(B):
+            win.net.set_state(b, th_pin[b], th_t[b], th_h[b])
+        win.t_end += w["window"]
+        win.net.set_horizon(win.t_end, w["dt"], False)
+        win.net.run()
+        rs = [win.net.order(b) for b in range(B)]
+        for b in range(B):
+            _, th_t[b], th_h[b] = win.net.state(b, out=th_pin[b])
+        e2e_s += time.perf_counter() - t0
+        e2e_units += win.net.stats()["accepted"] * n  # set_state restarts the per-trajectory counts
+        if it == 0:
+            h2d = 4 * n + 4 * n * B
+            d2h = sum(4 * r.size for r in rs) + 4 * n * B
+    e2e_units, e2e_ms = combine_ranks(e2e_units, e2e_s * 1e3, "cuda")
+    e2e_value = e2e_units / (e2e_ms / 1e3)
+    rec = win.rec
+    win.close()
+
+    # ---- the plain FP32 path on trajectory 0 of the same inputs
+    plain = None
+    if w.get("plain"):
+        pw = dict(WORKLOADS[w["plain"]])
+        pwin = Windowed(pw, thetas[:1], om, seed, local, stream.cuda_stream)
+        for _ in range(2):
+            pwin.horizon()
+            pwin.run()
+        pu, pms, pd = timed_windows(pwin, 2, stream)
+        pwin.close()
+        pval = pu / (pms / 1e3)
+        pk = pd["kernel_ms"] / max(pd["launches"], 1)
+        bytes_launch = 24.0 * n * pd["accepted"] * n / max(pd["launches"], 1)
+        plain = {"value": pval, "unit": "osc-steps/s", "windows": 2, "accepted_steps": pd["accepted"],
+                 "ratio_batched_over_plain": value / pval,
+                 "roofline": roofline_hbm(bytes_launch, pk)}
+    if rank != 0:
+        return
+    line = {"metric": metric, "value": value, "unit": "osc-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 state, bf16 split operands, f32 accumulation", "data": "synthetic",
+            "config": config}
+    line["e2e"] = {"value": e2e_value, "unit": "osc-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    # per attempt: coefficients, 6 x (stage phases, GEMM), error, decision, 2 output kernels
+    line["gpu_launches"] = 17 * d["launches"] + 6 * args.steps
+    line["roofline"] = roofline_tensor(n, B, d, ms) if w["engine"] == "tensor" else \
+        roofline_hbm(24.0 * n * d["accepted"] * n / max(d["launches"], 1), d["kernel_ms"] / max(d["launches"], 1))
+    line["clocks"] = clk.summary()
+    line["accepted_steps"] = {"timed": d["accepted"], "rejected": d["rejected"],
+                              "per_trajectory_per_window": d["accepted"] / B / args.steps,
+                              "t_reached": round(t_value_end, 4)}
+    if plain:
+        line["plain_fp32"] = plain
+    if not args.no_cpu:
+        v, el, st = window_cpu(w, thetas[0], om, w["cs"][0], CPU_WINDOWS * w["window"], threads)
+        line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
+                                "sample": "trajectory 0 from t=0 to t=%g (%d accepted steps, %.1f s), float32 oracle "
+                                          "restating the reference program, coupling in its rank-K form, OpenMP"
+                                          % (CPU_WINDOWS * w["window"], st, el)}
+        errs, cnt = [], 0
+        for b in sorted({0, B // 2, B - 1}):
+            ref, _ = fp64_records(w, thetas[b], om, w["cs"][b], t_value_end, threads)
+            common = [t for t in rec[b] if t in ref]
+            cnt += len(common)
+            if common:
+                errs.append(max(abs(float(rec[b][t]) - float(ref[t])) for t in common))
+        line["r_err_vs_fp64"] = max(errs) if errs else None
+        line["r_err_sample"] = ("trajectories %s, %d records at t <= %.3f against the FP64 oracle"
+                                % (sorted({0, B // 2, B - 1}), cnt, t_value_end))
+    print(json.dumps(line))
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def roofline_hbm(bytes_per_launch, kernel_ms_per_launch, traffic=None):
+    peaks = _peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    ach = bytes_per_launch / (kernel_ms_per_launch / 1e3) / 1e9 if kernel_ms_per_launch > 0 else 0.0
+    return {"bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4),
+            "traffic": traffic, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+            "kernel_ms_per_launch": round(kernel_ms_per_launch, 3)}
+
+
+def roofline_tensor(n, B, d, step_ms):
+    """The coupling GEMM: one launch is every trajectory's RHS, C = (N A) [cos|sin]: 4 N^2 B
+    algorithmic flops (2 columns x 2 flops per multiply-add), 8 N^2 B issued (hi and lo columns).
+    Its duration is the CUDA-event time of the GEMM launches the engine sampled in the timed
+    windows (event nodes around the six GEMMs of one attempt in four).  The GEMMs run back to
+    back through the whole window, so the sustained bf16 figure is the peak."""
+    peaks = _peaks()
+    peak = peaks.get("bf16_tflops_sustained", 1700.0)
+    src = "measured" if "bf16_tflops_sustained" in peaks else "fallback"
+    per = d["coupling_ms"] / max(d["coupling_launches"], 1)
+    flops = 4.0 * n * n * B
+    ach = flops / (per / 1e3) / 1e12 if per > 0 else 0.0
+    step_tf = 24.0 * n * d["accepted"] * n / (step_ms / 1e3) / 1e12 if step_ms > 0 else 0.0
+    return {"bound": "tensor", "achieved": round(ach, 1), "peak": peak, "unit": "TFLOP/s",
+            "frac": round(ach / peak, 4), "traffic": None, "peak_source": src,
+            "flops_per_launch": flops, "issued_flops_per_launch": 2 * flops,
+            "kernel_ms_per_launch": round(per, 4), "launches_sampled": d["coupling_launches"],
+            "whole_step_tflops": round(step_tf, 1), "whole_step_frac": round(step_tf / peak, 4)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="volcano200k", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ensemble65536", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--t1", type=float, default=None, help="shorter horizon (profiling captures only)")
     args = ap.parse_args()
@@ -598,6 +883,8 @@ def main():
         return main_multi(args, w)
     if w.get("kind") == "surrogate":
         return main_surrogate(args, w)
+    if w.get("kind") == "windows":
+        return main_windows(args, w)
     ws, rank, local = dist_env()
     n, B = w["n"], len(w["cs"])
     config = {"workload": args.workload, "n": n, "k": w["k"], "coupling": "volcano-regenerated" if w["coupling"] else

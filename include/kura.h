@@ -79,6 +79,9 @@ typedef struct kura_stats {
   double kernel_ms;    /* device time of the persistent launches (CUDA events) */
   int32_t grid;        /* CTAs of the persistent kernel */
   int32_t block;       /* threads per CTA */
+  double coupling_ms;  /* device time of the timed coupling-GEMM launches (tensor engine, environment
+                          KURA_TIME_COUPLING=1: the six GEMMs of one attempt in every four, CUDA events) */
+  int64_t coupling_launches; /* launches that coupling_ms covers */
 } kura_stats;
 
 /* Per-record observer callbacks, called from kura_run on the calling thread, in
@@ -118,7 +121,13 @@ int kura_set_state(kura_handle* h, int32_t traj, const float* theta, double t, d
 int kura_set_state_device(kura_handle* h, int32_t traj, const float* theta_device, double t, double step);
 /* output grid t_eval = dt*n, n = int(t0/dt)+1 .. int(t1/dt), and the end time
  * (kuramoto.cu:543-550); initial_record = 1 writes r(theta0) (and theta0,
- * couplings) first, as a fresh start does (kuramoto.cu:587-626) */
+ * couplings) first, as a fresh start does (kuramoto.cu:587-626).  After a kura_run that
+ * brought every trajectory to its end time, a new horizon continues the integration from
+ * where each trajectory stopped (phases, FSAL slope and step size kept on the device): the
+ * reference's -R resume (kuramoto.cu:466-494, 543) without the round trip through fs.dat.
+ * Trajectories of a batch may start (or continue) at different times: the grid then starts
+ * after the earliest one's time, and each trajectory records only the output times after
+ * its own. */
 int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t initial_record);
 
 /* integrate every trajectory to t1 (dp45_run with step_eval, dp45.cu:148-164) */
@@ -150,18 +159,22 @@ int kura_volcano_factor(int32_t seed, int64_t n, int32_t k, int8_t* u);
 /* Integrates `batch` trajectories of one volcano network with the factor
  * regenerated from Philox (the reference's -A mode) from t = 0 to t1, without
  * allocating any device memory.  No counterpart in the reference.  For callers
- * that cannot call cudaMalloc (a framework that owns the device allocator, a fixed
- * device-memory budget, code that must not allocate while a graph is captured).
+ * that cannot call cudaMalloc: a framework that owns the device allocator (its pool
+ * must account for every byte), or a process held to a fixed device-memory budget.
  * Inputs and outputs are the caller's device buffers: omega_dev[n];
- * theta_dev[batch][n] holds theta0 on entry and the final phases on return;
+ * theta_dev[batch][n] holds theta0 on entry and the final phases on success;
  * order_dev[batch][order_cap] receives r(0) and r at t = dt, 2dt, .., int(t1/dt)*dt.
  * c[batch] (coupling constants) is a host array; accepted (optional, host) gets the
- * accepted steps summed over the batch.  Scratch is one static __device__ array of
- * about 6.7 MiB held by every GPU that loads the library; it limits
- * round_up(n,32)*batch <= 65536, batch <= 8, k <= 32 and order_cap <= 4096, and larger
- * requests return KURA_ERR_INVALID.  All calls share that array: calls that overlap
- * on the GPU race.  The first call on a device looks up the array's address; make it
- * before any stream capture.  stream may be NULL (the legacy default stream). */
+ * accepted steps summed over the batch.  t1, dt, h0, atol and rtol must be finite.
+ * Scratch is one static __device__ array of about 6.7 MiB held by every GPU that
+ * loads the library; it limits round_up(n,32)*batch <= 65536, batch <= 8, k <= 32 and
+ * order_cap <= 4096, and larger requests return KURA_ERR_INVALID.  All calls share that
+ * array: calls that overlap on the GPU race.  The first call on a device looks up the
+ * array's address; make it before any stream capture.  The call waits for its work on
+ * `stream` before it returns (NULL: the legacy default stream) and leaves the caller's
+ * current device as it found it.  On an error return theta_dev still holds theta0,
+ * order_dev holds whatever records were written before the failure (not meaningful),
+ * and *accepted is not written. */
 int kura_integrate_volcano_noalloc(int64_t n, int32_t k, int32_t batch, int32_t seed, const float* c,
                                    const float* omega_dev, float* theta_dev, double t1, double dt, double h0,
                                    double atol, double rtol, int32_t device, void* stream, float* order_dev,

@@ -72,6 +72,7 @@ struct kura_handle {
   std::vector<float> c1;
   std::vector<float> t_eval_h;
   std::vector<double> t0;
+  std::vector<char> finished;  // the trajectory reached the end of a horizon (a later horizon continues it)
   bool omega_set = false, adj_set = false, horizon_set = false;
   long long launch_attempts = -1;  // step attempts per persistent launch (< 0: unbounded)
   // pinned host memory: the trajectory states and error flag of a launch in flight, and the
@@ -221,6 +222,7 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   for (auto& T : h->htraj) T.status = 1;  // no state yet
   h->c1.assign(h->B, 0.f);
   h->t0.assign(h->B, 0.0);
+  h->finished.assign(h->B, 0);
   h->order.assign(h->B, {});
   if (resolve_engine(cfg) == KURA_ENGINE_TENSOR) {
     h->te = new kura::TensorEngine();
@@ -287,6 +289,7 @@ extern "C" int kura_create(const kura_config* cfg, kura_handle** out) {
   }
   h->c1.assign(B, 0.f);
   h->t0.assign(B, 0.0);
+  h->finished.assign(B, 0);
   h->order.assign(B, {});
   h->stats.grid = G;
   h->stats.block = kura::KT;
@@ -416,6 +419,7 @@ static int set_state_common(kura_handle* h, int traj, const float* dev_theta, do
     CU(kura::launch_init_state(dev_theta, h->n, h->ld, h->ph_hi + off, h->ph_lo + off, h->ph_w + off, h->stream));
     CU(cudaStreamSynchronize(h->stream));
   }
+  h->finished[traj] = 0;
   TrajG& T = h->htraj[traj];
   float c = T.c1;
   T = TrajG{};
@@ -459,26 +463,48 @@ extern "C" int kura_set_state_device(kura_handle* h, int32_t traj, const float* 
 extern "C" int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t initial_record) {
   if (!h) return fail(KURA_ERR_INVALID, "handle is NULL");
   if (!(dt > 0)) return fail(KURA_ERR_INVALID, "dt must be > 0");
-  for (int b = 0; b < h->B; ++b)
-    if (h->htraj[b].status != 0 || h->htraj[b].need_k1 != 1)
-      return fail(KURA_ERR_INVALID, "set the state of every trajectory before the horizon");
-  for (int b = 1; b < h->B; ++b)
-    if (h->htraj[b].t != h->htraj[0].t) return fail(KURA_ERR_INVALID, "trajectories must start at the same time");
+  // either every trajectory has a fresh state (kura_set_state) or every one finished the
+  // previous horizon, which this one then continues from where it stopped
+  int fresh = 0, cont = 0;
+  for (int b = 0; b < h->B; ++b) {
+    const TrajG& T = h->htraj[b];
+    if (T.status == 0 && T.need_k1 == 1) fresh++;
+    else if (T.status == 1 && h->finished[b]) cont++;
+  }
+  if (fresh != h->B && cont != h->B)
+    return fail(KURA_ERR_INVALID, "set the state of every trajectory (or finish a run) before the horizon");
+  const bool continuing = cont == h->B;
+  double tmin = h->htraj[0].t;
+  for (int b = 1; b < h->B; ++b) tmin = std::min(tmin, h->htraj[b].t);
   CU(cudaSetDevice(h->cfg.device));
-  // t_eval = dt*n for n = int(t0/dt)+1 .. int(t1/dt), in float like the reference
-  float t0f = (float)h->htraj[0].t, dtf = (float)dt, t1f = (float)t1;
+  // t_eval = dt*n for n = int(t0/dt)+1 .. int(t1/dt), in float like the reference (a resumed
+  // run rebuilds it the same way from its start time, kuramoto.cu:543-550)
+  float t0f = (float)tmin, dtf = (float)dt, t1f = (float)t1;
   int n0 = int(t0f / dtf) + 1, n1 = int(t1f / dtf) + 1;
   h->t_eval_h.clear();
   for (int n = n0; n < n1; ++n) h->t_eval_h.push_back(dtf * n);
   h->n_eval = (int)h->t_eval_h.size();
+  // A trajectory that starts (or continues) after the earliest one owes no output at or
+  // before its own time.  A continued trajectory keeps its slopes (FSAL) and step size as
+  // after an accepted step.  Trajectories that start at the earliest time take the grid as
+  // the reference builds it, from its first point.
+  auto first_eval = [&](const TrajG& T) {
+    int e = 0;
+    if (continuing || T.t > tmin)
+      while (e < h->n_eval && T.t >= (double)h->t_eval_h[e]) e++;
+    return e;
+  };
+  for (int b = 0; b < h->B; ++b) {
+    if (continuing) h->htraj[b].status = 0;
+    h->finished[b] = 0;
+  }
   h->dt = dt;
   h->t1 = t1;
   if (h->te) {
     for (int b = 0; b < h->B; ++b) {
       TrajG& T = h->htraj[b];
       T.t1 = t1;
-      T.eval_i = 0;
-      T.eval_end = 0;
+      T.eval_i = T.eval_end = first_eval(T);
       T.need_init = initial_record ? 1 : 0;
       T.out_count = 0;
       T.log_count = 0;
@@ -520,8 +546,7 @@ extern "C" int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t in
   for (int b = 0; b < h->B; ++b) {
     TrajG& T = h->htraj[b];
     T.t1 = t1;
-    T.eval_i = 0;
-    T.eval_end = 0;
+    T.eval_i = T.eval_end = first_eval(T);
     T.need_init = initial_record ? 1 : 0;
     T.out_count = 0;
     T.log_count = 0;
@@ -628,6 +653,7 @@ extern "C" int kura_run(kura_handle* h, const kura_callbacks* cb) {
                                                       : "non-finite error norm";
       return fail(errc, m);
     }
+    for (int b = 0; b < h->B; ++b) h->finished[b] = h->htraj[b].status == 1;
     return KURA_OK;
   }
   const bool log_steps = cb && cb->on_step;
@@ -774,6 +800,7 @@ extern "C" int kura_run(kura_handle* h, const kura_callbacks* cb) {
   h->stats.accepted = acc;
   h->stats.rejected = rej;
   h->stats.barriers = bars;
+  for (int b = 0; b < h->B; ++b) h->finished[b] = h->htraj[b].status == 1;
   return KURA_OK;
 }
 

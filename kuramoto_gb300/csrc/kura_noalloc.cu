@@ -1,9 +1,10 @@
 // kura_noalloc.cu -- an integration entry point that allocates no device memory.
 //
 // Some callers cannot call cudaMalloc: code running inside a framework that owns
-// the device allocator (a memory pool that must see every allocation), a host
-// process with a fixed device-memory budget, or code under a CUDA graph capture
-// that must not allocate.  kura_integrate_volcano_noalloc serves them.  The caller
+// the device allocator (a memory pool that must see every allocation, so a private
+// cudaMalloc would fragment or overrun its budget), or a host process that runs
+// under a fixed device-memory budget set before it starts.
+// kura_integrate_volcano_noalloc serves them.  The caller
 // passes device buffers for its inputs and outputs; all scratch the persistent
 // kernel needs (phases, slopes, partial sums, the barrier counter, trajectory
 // state) lives in one file-scope __device__ array, g_noalloc_scratch, of TOTAL
@@ -19,9 +20,12 @@
 // on the GPU (concurrent streams, or host threads calling at once) race on the
 // array and corrupt each other's results: serialize them.  The first call on a
 // device looks up the array's device address (cudaGetSymbolAddress) with that
-// device current; make that first call before any stream capture.
+// device current; make that first call before any stream capture.  The call makes
+// `device` current while it works and restores the caller's current device on
+// every return.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -60,6 +64,17 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[TOTAL];
 
 std::mutex g_mu;
 void* g_addr[256];  // device address of g_noalloc_scratch per device ordinal
+
+// restores the caller's current device when the entry point returns
+struct DeviceRestore {
+  int dev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  }
+  ~DeviceRestore() {
+    if (dev >= 0) cudaSetDevice(dev);
+  }
+};
 
 int fail(int code, const std::string& m) {
   kura::set_last_error(m.c_str());  // read back with kura_last_error()
@@ -102,16 +117,27 @@ extern "C" int kura_integrate_volcano_noalloc(int64_t n, int32_t k, int32_t batc
   const long long ld = (n + 31) / 32 * 32;
   if (ld * batch > MAX_SLOTS)
     return fail(KURA_ERR_INVALID, "round_up(n,32)*batch exceeds the scratch limit of 65536");
-  if (!(dt > 0) || !(h0 > 0) || !(atol > 0) || rtol < 0) return fail(KURA_ERR_INVALID, "need dt, h0, atol > 0");
+  // every double must be finite (a NaN passes any ordered comparison's negation)
+  if (!std::isfinite(t1) || !std::isfinite(dt) || !std::isfinite(h0) || !std::isfinite(atol) ||
+      !std::isfinite(rtol))
+    return fail(KURA_ERR_INVALID, "t1, dt, h0, atol and rtol must be finite");
+  if (!(dt > 0) || !(h0 > 0) || !(atol > 0) || !(rtol >= 0) || !(t1 >= 0))
+    return fail(KURA_ERR_INVALID, "need dt, h0, atol > 0 and t1, rtol >= 0");
   if (order_cap < 1 || order_cap > MAX_RECORDS) return fail(KURA_ERR_INVALID, "order_cap must be in [1, 4096]");
-  // output grid t_eval = dt*n, n = 1 .. int(t1/dt) in float, as a fresh start of the reference
+  // output grid t_eval = dt*n, n = 1 .. int(t1/dt) in float, as a fresh start of the reference;
+  // the record count is bounded in floating point before any conversion to int
   const float dtf = (float)dt, t1f = (float)t1;
+  if (!(dtf > 0) || !std::isfinite(t1f) || !std::isfinite(t1f / dtf))
+    return fail(KURA_ERR_INVALID, "t1 and dt must be representable in float with dt > 0");
+  if (!((double)(t1f / dtf) < (double)order_cap))  // int(t1/dt) + 1 <= order_cap
+    return fail(KURA_ERR_INVALID, "order_cap smaller than the int(t1/dt)+1 records");
   const int n0 = 1, n1 = int(t1f / dtf) + 1;
   const int n_eval = n1 > n0 ? n1 - n0 : 0;
   if (n_eval + 1 > order_cap) return fail(KURA_ERR_INVALID, "order_cap smaller than the int(t1/dt)+1 records");
 
   cudaError_t e;
   if (device < 0 || device >= 256) return fail(KURA_ERR_INVALID, "device index out of range");
+  DeviceRestore restore;
   if ((e = cudaSetDevice(device)) != cudaSuccess) return fail(KURA_ERR_CUDA, cudaGetErrorString(e));
   unsigned char* base = nullptr;
   {

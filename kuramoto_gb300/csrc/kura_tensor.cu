@@ -516,6 +516,10 @@ struct TensorEngine::Impl {
   bool has_lo = false, adj_set = false;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // KURA_TIME_COUPLING=1: event nodes around the six coupling GEMMs of the attempt graph; the
+  // durations of the last replay of each batch of replays are summed into the stats
+  bool time_gemm = false;
+  cudaEvent_t gev[12] = {};
 };
 
 static std::string g_terr;
@@ -547,6 +551,8 @@ TensorEngine::~TensorEngine() {
   if (d->graph) cudaGraphExecDestroy(d->graph);
   if (d->ev0) cudaEventDestroy(d->ev0);
   if (d->ev1) cudaEventDestroy(d->ev1);
+  for (cudaEvent_t e : d->gev)
+    if (e) cudaEventDestroy(e);
   delete d;
 }
 
@@ -582,6 +588,10 @@ int TensorEngine::init(int64_t n, int k, int batch, int seed, double atol, doubl
   TCU(cudaHostAlloc((void**)&I.h_done, sizeof(int), cudaHostAllocDefault));
   TCU(cudaEventCreate(&I.ev0));
   TCU(cudaEventCreate(&I.ev1));
+  const char* tg = getenv("KURA_TIME_COUPLING");
+  I.time_gemm = tg && atoi(tg) != 0;
+  if (I.time_gemm)
+    for (cudaEvent_t& e : I.gev) TCU(cudaEventCreate(&e));
   // X is [4 bp][np]: a work unit's column block is 4 * x_bph(bp) rows (its hi + lo columns),
   // of which the A_lo pass reads the first half
   if (make_tmap_bf16(&I.tmA, I.Ahi, np, np, TG_BM) || make_tmap_bf16(&I.tmX, I.X, np, 4 * bp, 4 * x_bph(I.bp)) ||
@@ -734,14 +744,19 @@ static cudaError_t gemm(TensorEngine::Impl& I, const TCoef* src, int mode, const
   }
 }
 
-static cudaError_t coupling(TensorEngine::Impl& I, const TCoef* src, int mode, float* fin_theta, const int* run_flag) {
+static cudaError_t coupling(TensorEngine::Impl& I, const TCoef* src, int mode, float* fin_theta, const int* run_flag,
+                            int timed = -1) {
   TView v{I.n, I.np, I.bp, I.B, mode, I.omega, I.ph_hi, I.ph_lo, I.ph_w, I.g, I.X, I.x32, fin_theta, I.fin_coup,
           I.Flo};
   dim3 grid((unsigned)((I.n + 255) / 256), (unsigned)I.B);
   k_t_stage<<<grid, 256, 0, I.st>>>(v, src);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return gemm(I, src, mode, run_flag);
+  const bool tm = I.time_gemm && timed >= 0;
+  if (tm && (e = cudaEventRecordWithFlags(I.gev[2 * timed], I.st, cudaEventRecordExternal)) != cudaSuccess) return e;
+  if ((e = gemm(I, src, mode, run_flag)) != cudaSuccess) return e;
+  if (tm) e = cudaEventRecordWithFlags(I.gev[2 * timed + 1], I.st, cudaEventRecordExternal);
+  return e;
 }
 
 // one attempt of every trajectory, then its outputs
@@ -751,7 +766,7 @@ static cudaError_t attempt(TensorEngine::Impl& I) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   for (int s = 2; s <= 7; ++s) {
-    e = coupling(I, I.src + (size_t)(s - 1) * I.bp, 0, nullptr, I.any_active + 1);
+    e = coupling(I, I.src + (size_t)(s - 1) * I.bp, 0, nullptr, I.any_active + 1, s - 2);
     if (e != cudaSuccess) return e;
   }
   if (!I.fixed) {
@@ -808,6 +823,15 @@ int TensorEngine::run(std::vector<TrajG>& traj, kura_stats& stats) {
     TCU(cudaMemcpy(&errv, I.err, sizeof(int), cudaMemcpyDeviceToHost));
     if (errv) { g_terr = "tensor GEMM aborted (wait time limit)"; return KURA_ERR_BARRIER_TIMEOUT; }
     if (*I.h_done) break;
+    if (I.time_gemm) {  // every replay of this batch stepped some trajectory: sample the last one
+      for (int q = 0; q < 6; ++q) {
+        float gm = 0.f;
+        if (cudaEventElapsedTime(&gm, I.gev[2 * q], I.gev[2 * q + 1]) == cudaSuccess) {
+          stats.coupling_ms += gm;
+          stats.coupling_launches++;
+        }
+      }
+    }
   }
   TCU(cudaEventRecord(I.ev1, I.st));
   TCU(cudaMemcpyAsync(traj.data(), I.traj, sizeof(TrajG) * I.B, cudaMemcpyDeviceToHost, I.st));

@@ -46,7 +46,7 @@ class Stats(ctypes.Structure):
     _fields_ = [
         ("accepted", ctypes.c_int64), ("rejected", ctypes.c_int64), ("launches", ctypes.c_int64),
         ("barriers", ctypes.c_int64), ("kernel_ms", ctypes.c_double), ("grid", ctypes.c_int32),
-        ("block", ctypes.c_int32),
+        ("block", ctypes.c_int32), ("coupling_ms", ctypes.c_double), ("coupling_launches", ctypes.c_int64),
     ]
 
 

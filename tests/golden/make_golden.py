@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures under tests/golden/ from the reference checkout.
 
-Run in a container that has the reference at REFERENCE (default /root/reference):
-    python tests/golden/make_golden.py
+Give the reference checkout as the argument (or in the REFERENCE environment variable):
+    python tests/golden/make_golden.py REFERENCE_DIR
 The fixtures are data files of the reference repository (znicolaou/kuramoto,
 data/), copied byte for byte, plus their SHA-256 digests:
   * {normal,cauchy}_K{0,2,5000}_seed1_frequencies.dat  -- frequencies.dat of seed 1, N=5000
@@ -17,7 +17,7 @@ import os
 import shutil
 import sys
 
-REF = os.environ.get("REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 FILES = {}
@@ -34,6 +34,8 @@ FILES["normal_N10000_K2000_avgorder.npy"] = "data/10000/2000/avgorder.npy"
 
 
 def main():
+    if not REF:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_DIR")
     if not os.path.isdir(REF):
         sys.exit("reference checkout not found: %s" % REF)
     digests = {}

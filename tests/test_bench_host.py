@@ -47,15 +47,27 @@ def test_int8_roofline_counts_one_byte_per_entry():
     assert abs(r["bytes_per_unit"] - 6.0 * n) < 1e-6
 
 
-def test_tensor_roofline_counts_algorithmic_flops():
+def test_tensor_roofline_counts_algorithmic_flops_per_gemm_launch():
     w = bench.WORKLOADS["ensemble65536"]
-    n = w["n"]
-    acc = 700  # accepted steps summed over the batch, one integration
-    r = bench.roofline(w, dict(kernel_ms=2 * 114.5, launches=8, acc_per_step=acc), _args("ensemble65536", 2))
-    expect = 24.0 * n * acc * n / 0.1145 / 1e12
+    n, B = w["n"], len(w["cs"])
+    d = dict(accepted=128 * 70, coupling_ms=6 * 2.9, coupling_launches=6)
+    r = bench.roofline_tensor(n, B, d, step_ms=1500.0)
+    flops = 4.0 * n * n * B  # one RHS of every trajectory: 2 columns x 2 flops x N^2
     assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
-    assert abs(r["achieved"] - round(expect, 2)) < 0.011
-    assert r["issued_flops_per_unit"] == 2 * r["flops_per_unit"] == 48.0 * n
+    assert abs(r["achieved"] - round(flops / 2.9e-3 / 1e12, 1)) < 0.051
+    assert r["issued_flops_per_launch"] == 2 * r["flops_per_launch"] == 2 * flops
+    assert abs(r["whole_step_tflops"] - round(24.0 * n * 128 * 70 * n / 1.5 / 1e12, 1)) < 0.051
+
+
+def test_window_inputs_share_trajectory_zero():
+    from oracle import kora
+    w = bench.WORKLOADS["ensemble65536"]
+    small = dict(w, n=1000, cs=[3.0] * 4)
+    th4, om4 = bench.window_inputs(small, 1, kora.host_random_inputs)
+    th1, om1 = bench.window_inputs(dict(small, cs=[3.0]), 1, kora.host_random_inputs)
+    assert np.array_equal(th4[0], th1[0]) and np.array_equal(om4, om1)
+    assert all(t.min() >= 0 and t.max() < 2 * np.pi for t in th4)
+    assert not np.array_equal(th4[0], th4[1])
 
 
 def test_volcano_roofline_uses_the_state_bytes():

@@ -29,14 +29,20 @@ def _entry(native):
     return f
 
 
-def test_noalloc_matches_handle_api_twice(native):
+# (batch, k, side stream): the batch-1 and batch-8 kernels, the rank-8 and rank-32 factor
+# caches, and a caller's own stream next to the legacy default stream
+CASES = [(3, 5, False), (1, 5, True), (2, 20, True)]
+
+
+@pytest.mark.parametrize("batch,k,side_stream", CASES)
+def test_noalloc_matches_handle_api_twice(native, batch, k, side_stream):
     import torch
 
-    n, k, seed, t1, dt, h0 = 3000, 5, 7, 6.0, 0.5, 0.005
-    cs = [1.5, 3.0, 4.5]
+    n, seed, t1, dt, h0 = 3000, 7, 6.0, 0.5, 0.005
+    cs = [1.5, 3.0, 4.5][:batch]
     B = len(cs)
     th, om = normal_inputs(n, 19)
-    thetas = [th, (th + 0.3).astype(np.float32), (th * 0.5).astype(np.float32)]
+    thetas = [th, (th + 0.3).astype(np.float32), (th * 0.5).astype(np.float32)][:B]
 
     net = native.Network(n, k=k, coupling=native.COUPLING_VOLCANO, batch=B, seed=seed, dense_level=0)
     net.set_frequencies(om)
@@ -58,14 +64,17 @@ def test_noalloc_matches_handle_api_twice(native):
     cap = 64
     c_arr = (ctypes.c_float * B)(*cs)
     om_d = torch.from_numpy(om).cuda()
+    stream = torch.cuda.Stream() if side_stream else None
     for call in range(2):
         th_d = torch.from_numpy(np.stack(thetas)).cuda().contiguous()
         r_d = torch.full((B, cap), -1.0, dtype=torch.float32, device="cuda")
         acc = ctypes.c_int64(0)
         torch.cuda.synchronize()
-        rc = f(n, k, B, seed, c_arr, om_d.data_ptr(), th_d.data_ptr(), t1, dt, h0, 1e-6, 0.0, 0, None,
+        rc = f(n, k, B, seed, c_arr, om_d.data_ptr(), th_d.data_ptr(), t1, dt, h0, 1e-6, 0.0, 0,
+               ctypes.c_void_p(stream.cuda_stream) if stream is not None else None,
                r_d.data_ptr(), cap, ctypes.byref(acc))
         assert rc == 0, native.lib().kura_last_error().decode()
+        assert torch.cuda.current_device() == 0
         r = r_d.cpu().numpy()
         fin = th_d.cpu().numpy()
         assert acc.value == ref_acc
@@ -92,3 +101,22 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(native):
     rc = f(1000, 5, 1, 1, c_arr, om_d.data_ptr(), th_d.data_ptr(), 100.0, 1.0, 0.01, 1e-6, 0.0, 0, None,
            r_d.data_ptr(), 16, None)
     assert rc == -1 and "order_cap" in native.lib().kura_last_error().decode()
+
+
+def test_noalloc_rejects_non_finite_or_oversized_horizons(native):
+    """Each of these returns before any device work: the checks are on the host."""
+    import torch
+
+    f = _entry(native)
+    om_d = torch.zeros(100, device="cuda")
+    th_d = torch.zeros(100, device="cuda")
+    r_d = torch.zeros(16, device="cuda")
+    c_arr = (ctypes.c_float * 1)(1.0)
+    nan, inf = float("nan"), float("inf")
+    bad = [(nan, 1.0, 0.01, 1e-6, 0.0), (inf, 1.0, 0.01, 1e-6, 0.0), (1e30, 1e-30, 0.01, 1e-6, 0.0),
+           (1e12, 1.0, 0.01, 1e-6, 0.0), (1.0, 1.0, nan, 1e-6, 0.0), (1.0, 1.0, 0.01, 1e-6, nan),
+           (1.0, nan, 0.01, 1e-6, 0.0), (-1.0, 1.0, 0.01, 1e-6, 0.0)]
+    for t1, dt, h0, atol, rtol in bad:
+        rc = f(100, 5, 1, 1, c_arr, om_d.data_ptr(), th_d.data_ptr(), t1, dt, h0, atol, rtol, 0, None,
+               r_d.data_ptr(), 16, None)
+        assert rc == -1, (t1, dt, h0, atol, rtol)
