@@ -52,13 +52,22 @@ WORKLOADS = {
                          atol=1e-6, rtol=0.0, shared_theta=False, adj_storage=1),
     # the shared-adjacency ensemble on tensor cores: N=65536, K=5 dense volcano adjacency,
     # 128 trajectories with distinct theta0 uniform in [0, 2pi), shared Cauchy omega, c=3,
-    # integrated toward t=20 with records every 0.01; one bench step is a window of 0.05 time
-    # units that continues the same integration (warm-up windows start it from t=0).  The
-    # plain FP32 path (`dense65536w`) runs trajectory 0 of the same inputs beside it.
+    # integrated toward t=20 with records every 0.01; one bench step is a window of 0.8 time
+    # units that continues the same integration (warm-up windows start it from t=0), so the
+    # default 5 warm-up and 20 timed steps cover t = 0..20.  The plain FP32 path
+    # (`dense65536w`) runs trajectory 0 of the same inputs beside it.
     "ensemble65536": dict(kind="windows", n=65536, k=5, cs=[3.0] * 128, init=2 * np.pi, t1=20.0, dt=0.01,
-                          window=0.05, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
-    "dense65536w": dict(kind="windows", n=65536, k=5, cs=[3.0], init=2 * np.pi, t1=20.0, dt=0.01, window=0.05,
+                          window=0.8, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
+    "dense65536w": dict(kind="windows", n=65536, k=5, cs=[3.0], init=2 * np.pi, t1=20.0, dt=0.01, window=0.8,
                         atol=1e-6, rtol=0.0, engine="persistent"),
+    # the same ensemble at N=32768 (a 2.1 GB BF16 adjacency, larger than L2): profiling captures
+    "ensemble32768": dict(kind="windows", n=32768, k=5, cs=[3.0] * 128, init=2 * np.pi, t1=20.0, dt=0.01,
+                          window=0.8, atol=1e-6, rtol=0.0, engine="tensor"),
+    # a batch of 8 on either engine (the choice KURA_ENGINE_AUTO makes for small dense batches)
+    "ensemble65536x8": dict(kind="windows", n=65536, k=5, cs=[3.0] * 8, init=2 * np.pi, t1=20.0, dt=0.01,
+                            window=0.8, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
+    "dense65536x8w": dict(kind="windows", n=65536, k=5, cs=[3.0] * 8, init=2 * np.pi, t1=20.0, dt=0.01,
+                          window=0.8, atol=1e-6, rtol=0.0, engine="persistent"),
     # the same ensemble at N=16384 (a 512 MiB BF16 adjacency, still larger than L2): profiling captures
     "ensemble16384": dict(n=16384, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
                           dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False, engine="tensor"),
@@ -577,6 +586,45 @@ def cpu_baseline(w, om, thetas, threads, sample_steps=None):
     return steps * n / el, el, steps
 
 
+def volcano_accuracy(w, thetas, om, seed, device, threads, t_phase=10.0):
+    """The accuracy contract of the large regenerated network, for every c of the batch: phases
+    within 1e-4 rad of the FP64 oracle for t <= t_phase (plus one float32 ulp of the phase), and
+    the time-averaged r within 1e-3 over the whole horizon.  One extra GPU integration with the
+    phases recorded at every output time; the FP64 oracle runs each trajectory on the host."""
+    import kuramoto_gb300 as kg
+    from oracle import kora
+    n, B = w["n"], len(w["cs"])
+    net = kg.Network(n, k=w["k"], coupling=w["coupling"], batch=B, seed=seed, atol=w["atol"], rtol=w["rtol"],
+                     dense_level=1, device=device)
+    net.set_frequencies(om)
+    for b, c in enumerate(w["cs"]):
+        net.set_coupling(b, c)
+        net.set_state(b, thetas[b], 0.0, w["dt"] / 100)
+    net.set_horizon(w["t1"], w["dt"], True)
+    rows = int(round(t_phase / w["dt"])) + 1  # records at t = 0, dt, .., t_phase
+    th_gpu = {b: [] for b in range(B)}
+    net.run(on_output=lambda b, i, te, r, th, cp: (len(th_gpu[b]) < rows and th_gpu[b].append(th)) and False)
+    r_gpu = [net.order(b) for b in range(B)]
+    net.close()
+    per_c = []
+    for b, c in enumerate(w["cs"]):
+        ref = kora.run(thetas[b], om, k=w["k"], c1=c, onthefly=w["coupling"] == 1, seed=seed, fp64=True, t1=w["t1"],
+                       dt=w["dt"], atol=w["atol"], rtol=w["rtol"], dense=1, threads=threads)
+        tg = np.stack(th_gpu[b]).astype(np.float64)
+        tr = ref.thetas[:rows]
+        d = np.abs((tg - tr + np.pi) % (2 * np.pi) - np.pi)
+        ulp = np.spacing(np.abs(tr).astype(np.float32)).astype(np.float64)
+        m = min(r_gpu[b].size, ref.order.size)
+        per_c.append({"c": c, "theta_err_max_t_le_%g" % t_phase: float(d.max()),
+                      "theta_err_over_1e-4_plus_ulp": float((d - 1e-4 - ulp).max()),
+                      "r_err_max": float(np.max(np.abs(r_gpu[b][:m] - ref.order[:m]))),
+                      "mean_r_err": float(abs(np.mean(r_gpu[b][:m], dtype=np.float64) - np.mean(ref.order[:m])))})
+    return {"vs": "FP64 oracle (rank-K coupling, the reference's -A arithmetic in double)",
+            "theta_window": [0.0, t_phase], "r_window": [0.0, w["t1"]], "per_c": per_c,
+            "max_theta_err": max(x["theta_err_max_t_le_%g" % t_phase] for x in per_c),
+            "max_mean_r_err": max(x["mean_r_err"] for x in per_c)}
+
+
 def r_error_vs_fp64(w, om, theta, c, gpu_order, threads, t1=3.0):
     """max |r_gpu - r_fp64| over the first outputs (the FP64 oracle on a bounded horizon)."""
     from oracle import kora
@@ -588,11 +636,12 @@ def r_error_vs_fp64(w, om, theta, c, gpu_order, threads, t1=3.0):
 
 # ------------------------------------------------------------------ windowed workloads
 def window_inputs(w, seed, host_rng):
-    """Shared Cauchy omega (glibc rand of `seed`, scale 1, the reference's generator) and one
-    theta0 per trajectory, uniform in [0, init), from a numpy stream of `seed`.  Trajectory 0 is
-    the same for every batch size, so the plain path integrates the ensemble's first member."""
+    """Shared Cauchy omega of scale 1 as the reference draws it on a fresh start (glibc rand of
+    `seed`, N draws for theta0 first: its frequencies.dat) and one theta0 per trajectory, uniform
+    in [0, init), from a numpy stream of `seed`.  Trajectory 0 is the same for every batch size,
+    so the plain path integrates the ensemble's first member."""
     n, B = w["n"], len(w["cs"])
-    _, om = host_rng(seed, n, 0.0, 1.0, False, gen_theta=False)
+    _, om = host_rng(seed, n, 0.0, 1.0, False)
     rng = np.random.default_rng(seed)
     return [(rng.random(n) * w["init"]).astype(np.float32) for _ in range(B)], om
 
@@ -653,29 +702,36 @@ def timed_windows(win, steps, stream, clocks=None):
     return d["accepted"] * win.n, ms, d
 
 
-def fp64_records(w, theta0, om, c, t1, threads):
+def fp64_records(w, theta0, om, c, t1, threads, seed=1):
     """r of one trajectory from the FP64 oracle (rank-K form: the same matrix as the stored
     dense volcano adjacency, at O(N K) per RHS) at t = 0, dt, .., keyed like the GPU records."""
     from oracle import kora
-    r = kora.run(theta0, om, k=w["k"], c1=c, onthefly=True, seed=1, fp64=True, t1=t1, dt=w["dt"], atol=w["atol"],
-                 rtol=w["rtol"], threads=threads)
+    r = kora.run(theta0, om, k=w["k"], c1=c, onthefly=True, seed=seed, fp64=True, t1=t1, dt=w["dt"],
+                 atol=w["atol"], rtol=w["rtol"], threads=threads)
     keys = [round(float(np.float32(np.float32(w["dt"]) * np.float32(i))), 9) for i in range(r.order.size)]
     keys[0] = 0.0
     return dict(zip(keys, r.order)), r.steps
 
 
-def window_cpu(w, theta0, om, c, t1, threads):
-    """The float32 oracle port of the reference program on one trajectory from t = 0 to t1, the
-    coupling in its rank-K form (kuramoto.cu:62-101 arithmetic; the same matrix as the dense A)."""
+def window_cpu_model(w, om, threads):
+    """The float32 oracle port of the reference program holding the workload's dense volcano
+    adjacency (4 N^2 bytes of host memory, built once), as the reference stores it and streams
+    it twice per RHS (two GEMVs, kuramoto.cu:113-114)."""
     from oracle import kora
     t0 = time.perf_counter()
-    r = kora.run(theta0, om, k=w["k"], c1=c, onthefly=True, seed=1, fp64=False, t1=t1, dt=w["dt"], atol=w["atol"],
-                 rtol=w["rtol"], threads=threads)
+    M = kora.Model(om, k=w["k"], seed=1, fp64=False, threads=threads)
+    return M, time.perf_counter() - t0
+
+
+def window_cpu(w, M, theta0, c, attempts):
+    """`attempts` step attempts of one trajectory from t = 0 on the CPU port."""
+    t0 = time.perf_counter()
+    r = M.run(theta0, c1=c, t1=w["t1"], dt=w["dt"], atol=w["atol"], rtol=w["rtol"], max_attempts=attempts)
     el = time.perf_counter() - t0
     return r.steps * w["n"] / el, el, r.steps
 
 
-CPU_WINDOWS = 4  # the CPU sample: one trajectory over this many windows from t = 0
+CPU_ATTEMPTS = 2  # the CPU sample: step attempts of one trajectory from t = 0 (dense FP32 port)
 
 
 def main_windows(args, w):
@@ -693,20 +749,23 @@ def main_windows(args, w):
               "l2": "inputs larger than L2 (the adjacency, %.1f GB, is streamed by every RHS); not flushed"
                     % (n * n * (2 if w["engine"] == "tensor" else 4) / 1e9),
               "parallelism": "replicas" if ws > 1 else "single"}
-    sample = ("trajectory b = step mod %d from t=0 to t=%g (%d windows), float32 oracle restating the reference "
-              "program, coupling in its rank-K form, OpenMP" % (B, CPU_WINDOWS * w["window"], CPU_WINDOWS))
+    sample = ("trajectory b = step mod %d, %d step attempts from t=0, float32 oracle restating the reference "
+              "program with the dense adjacency in host memory (two GEMV passes per RHS), OpenMP"
+              % (B, CPU_ATTEMPTS))
     if args.impl == "reference":
         if rank != 0:
             return
         from oracle import kora
         thetas, om = window_inputs(w, 1, kora.host_random_inputs)
+        M, _ = window_cpu_model(w, om, threads)
         for i in range(args.warmup):
-            window_cpu(w, thetas[i % B], om, w["cs"][i % B], w["window"], threads)
+            window_cpu(w, M, thetas[i % B], w["cs"][i % B], 1)
         units = el = 0.0
         for i in range(args.steps):
-            v, e, st = window_cpu(w, thetas[i % B], om, w["cs"][i % B], CPU_WINDOWS * w["window"], threads)
+            v, e, st = window_cpu(w, M, thetas[i % B], w["cs"][i % B], CPU_ATTEMPTS)
             units += st * n
             el += e
+        M.close()
         value = units / el
         print(json.dumps({"impl": "reference", "metric": metric, "value": value, "unit": "osc-steps/s",
                           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -718,6 +777,8 @@ def main_windows(args, w):
                                   "d2h_bytes_per_step": 0}}))
         return
 
+    if args.until is not None:
+        args.steps = max(1, int(round(args.until / w["window"])) - args.warmup)
     import torch
     import kuramoto_gb300 as kg
     os.environ.setdefault("KURA_TIME_COUPLING", "1")
@@ -756,7 +817,7 @@ def main_windows(args, w):
         _, th_t[b], th_h[b] = win.net.state(b, out=th_pin[b])
     e2e_units = e2e_s = 0.0
     h2d = d2h = 0
-    for it in range(args.steps):
+    for it in range(0 if args.no_e2e else args.steps):
         barrier()
         t0 = time.perf_counter()
         win.net.set_frequencies(om_pin)
@@ -774,7 +835,7 @@ def main_windows(args, w):
             h2d = 4 * n + 4 * n * B
             d2h = sum(4 * r.size for r in rs) + 4 * n * B
     e2e_units, e2e_ms = combine_ranks(e2e_units, e2e_s * 1e3, "cuda")
-    e2e_value = e2e_units / (e2e_ms / 1e3)
+    e2e_value = e2e_units / (e2e_ms / 1e3) if e2e_ms > 0 else None
     rec = win.rec
     win.close()
 
@@ -801,10 +862,16 @@ def main_windows(args, w):
             "vs_baseline": None, "dtype": "f32 state, bf16 split operands, f32 accumulation", "data": "synthetic",
             "config": config}
     line["e2e"] = {"value": e2e_value, "unit": "osc-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-    # per attempt: coefficients, 6 x (stage phases, GEMM), error, decision, 2 output kernels
-    line["gpu_launches"] = 17 * d["launches"] + 6 * args.steps
-    line["roofline"] = roofline_tensor(n, B, d, ms) if w["engine"] == "tensor" else \
-        roofline_hbm(24.0 * n * d["accepted"] * n / max(d["launches"], 1), d["kernel_ms"] / max(d["launches"], 1))
+    if w["engine"] == "tensor":
+        # per attempt: coefficients, 6 x (stage phases, GEMM), error, decision, 2 output kernels;
+        # per window: the first slope's 6 kernels
+        line["gpu_launches"] = 17 * d["launches"] + 6 * args.steps
+        line["roofline"] = roofline_tensor(n, B, d, ms)
+    else:
+        # one persistent launch per window; A is read once per RHS for the whole batch
+        line["gpu_launches"] = d["launches"]
+        line["roofline"] = roofline_hbm(24.0 * n * n * d["accepted"] / B / max(d["launches"], 1),
+                                        d["kernel_ms"] / max(d["launches"], 1))
     line["clocks"] = clk.summary()
     line["accepted_steps"] = {"timed": d["accepted"], "rejected": d["rejected"],
                               "per_trajectory_per_window": d["accepted"] / B / args.steps,
@@ -812,14 +879,17 @@ def main_windows(args, w):
     if plain:
         line["plain_fp32"] = plain
     if not args.no_cpu:
-        v, el, st = window_cpu(w, thetas[0], om, w["cs"][0], CPU_WINDOWS * w["window"], threads)
+        M, build_s = window_cpu_model(w, om, threads)
+        v, el, st = window_cpu(w, M, thetas[0], w["cs"][0], CPU_ATTEMPTS)
+        M.close()
         line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
-                                "sample": "trajectory 0 from t=0 to t=%g (%d accepted steps, %.1f s), float32 oracle "
-                                          "restating the reference program, coupling in its rank-K form, OpenMP"
-                                          % (CPU_WINDOWS * w["window"], st, el)}
+                                "sample": "trajectory 0, %d step attempts from t=0 (%d accepted, %.1f s; the dense "
+                                          "adjacency built once beforehand in %.1f s), float32 oracle restating the "
+                                          "reference program, two GEMV passes per RHS, OpenMP"
+                                          % (CPU_ATTEMPTS, st, el, build_s)}
         errs, cnt = [], 0
         for b in sorted({0, B // 2, B - 1}):
-            ref, _ = fp64_records(w, thetas[b], om, w["cs"][b], t_value_end, threads)
+            ref, _ = fp64_records(w, thetas[b], om, w["cs"][b], t_value_end, threads, seed)
             common = [t for t in rec[b] if t in ref]
             cnt += len(common)
             if common:
@@ -859,11 +929,26 @@ def roofline_tensor(n, B, d, step_ms):
     flops = 4.0 * n * n * B
     ach = flops / (per / 1e3) / 1e12 if per > 0 else 0.0
     step_tf = 24.0 * n * d["accepted"] * n / (step_ms / 1e3) / 1e12 if step_ms > 0 else 0.0
-    return {"bound": "tensor", "achieved": round(ach, 1), "peak": peak, "unit": "TFLOP/s",
-            "frac": round(ach / peak, 4), "traffic": None, "peak_source": src,
-            "flops_per_launch": flops, "issued_flops_per_launch": 2 * flops,
-            "kernel_ms_per_launch": round(per, 4), "launches_sampled": d["coupling_launches"],
-            "whole_step_tflops": round(step_tf, 1), "whole_step_frac": round(step_tf / peak, 4)}
+    # the adjacency (N*A in BF16) is read once per launch: a small batch makes the launch HBM-bound
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    a_gbs = 2.0 * n * n / (per / 1e3) / 1e9 if per > 0 else 0.0
+    out = {"bound": "tensor", "achieved": round(ach, 1), "peak": peak, "unit": "TFLOP/s",
+           "frac": round(ach / peak, 4), "traffic": None, "peak_source": src,
+           "flops_per_launch": flops, "issued_flops_per_launch": 2 * flops,
+           "kernel_ms_per_launch": round(per, 4), "launches_sampled": d["coupling_launches"],
+           "whole_step_tflops": round(step_tf, 1), "whole_step_frac": round(step_tf / peak, 4),
+           "adjacency_gbs": round(a_gbs, 1), "adjacency_hbm_frac": round(a_gbs / hbm, 4)}
+    bp = 16
+    while bp < B:
+        bp *= 2
+    issued = 8.0 * n * n * bp  # hi and lo columns of the padded batch
+    out["issued_flops_per_launch"] = issued
+    out["issued_frac"] = round(issued / (per / 1e3) / 1e12 / peak, 4) if per > 0 else 0.0
+    if a_gbs / hbm > out["issued_frac"]:
+        out.update({"bound": "hbm", "achieved": round(a_gbs, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(a_gbs / hbm, 4), "tensor_frac": round(ach / peak, 4),
+                    "bytes_per_launch": 2.0 * n * n})
+    return out
 
 
 def main():
@@ -875,6 +960,9 @@ def main():
     ap.add_argument("--workload", default="ensemble65536", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--t1", type=float, default=None, help="shorter horizon (profiling captures only)")
+    ap.add_argument("--until", type=float, default=None,
+                    help="windowed workloads: time windows until the integration reaches this t (e.g. 20)")
+    ap.add_argument("--no-e2e", action="store_true", help="windowed workloads: skip the host-buffer leg")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.t1 is not None:
@@ -940,9 +1028,14 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
                                 "sample": "whole workload (%d trajectories to t=%g, %d accepted steps, %.1f s), "
                                           "float32 oracle restating the reference program" % (B, w["t1"], steps, el)}
-        ci = len(w["cs"]) // 2
-        line["r_err_vs_fp64"] = r_error_vs_fp64(w, res["om"], res["thetas"][ci], w["cs"][ci], res["orders"][ci],
-                                                threads)
+        if w["coupling"] == 1:
+            acc = volcano_accuracy(w, res["thetas"], res["om"], instance_seed(res["rank"]), 0, threads)
+            line["accuracy"] = acc
+            line["r_err_vs_fp64"] = max(x["r_err_max"] for x in acc["per_c"])
+        else:
+            ci = len(w["cs"]) // 2
+            line["r_err_vs_fp64"] = r_error_vs_fp64(w, res["om"], res["thetas"][ci], w["cs"][ci], res["orders"][ci],
+                                                    threads)
     print(json.dumps(line))
 
 

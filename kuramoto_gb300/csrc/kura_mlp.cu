@@ -305,7 +305,7 @@ constexpr unsigned long long GEMM_LIMIT_NS = 20000000000ull;
 template <int NCOL, class Epi>
 cudaError_t gemm(kura_mlp* m, const CUtensorMap& a, const CUtensorMap& x, int mtiles, int ktiles, const Epi& e) {
   kura::k_tensor_gemm<NCOL, Epi><<<std::min(mtiles, m->sms), kura::TG_THREADS, kura::TGCfg<NCOL>::SMEM, m->st>>>(
-      a, x, mtiles, ktiles, 1, 0, e, m->err, GEMM_LIMIT_NS, nullptr);
+      a, x, mtiles, mtiles, ktiles, 1, 0, e, m->err, GEMM_LIMIT_NS, nullptr);
   return cudaGetLastError();
 }
 

@@ -713,15 +713,26 @@ static cudaError_t launch_gemm(TensorEngine::Impl& I, const TCoef* src, int mode
   constexpr int BP = NCOL / 4;  // trajectories per work unit
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, I.device);
-  const int mtiles = I.np / (2 * TG_BM), ktiles = I.np / TG_BK;  // units of two row tiles
+  const int mtiles = I.np / (2 * TG_BM), ktiles = I.np / TG_BK;  // groups of two row tiles
   const int nsplit = I.bp / BP, xstride = 4 * BP;
   const int grid = std::min(mtiles * nsplit, sms);
+  // Units of two row tiles fill whole waves of the grid; the rest run as one-tile units, when
+  // that shortens the last wave (in unit times: a one-tile unit is half of a two-tile one)
+  int big = mtiles;
+  {
+    const int full = (mtiles * nsplit) / grid;
+    const int b = full * grid / nsplit;
+    const int tail = (mtiles - b) * 2 * nsplit;
+    const double t_split = full + 0.5 * ((tail + grid - 1) / grid);
+    const double t_big = (mtiles * nsplit + grid - 1) / grid;
+    if (b < mtiles && t_split < t_big) big = b;
+  }
   const unsigned long long limit = 20000000000ull;
   if (I.has_lo) {
     auto kl = k_tensor_gemm<NCOL / 2, LoEpi<BP>, 2>;
     cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL / 2, 2>::SMEM);
     LoEpi<BP> le{v, src};
-    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2, 2>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, ktiles, nsplit, xstride, le,
+    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2, 2>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, big, ktiles, nsplit, xstride, le,
                                                              I.err, limit, run_flag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -729,7 +740,7 @@ static cudaError_t launch_gemm(TensorEngine::Impl& I, const TCoef* src, int mode
   auto k = k_tensor_gemm<NCOL, KuraEpi<BP>, 2>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL, 2>::SMEM);
   KuraEpi<BP> ep{v, src, 1.0f / (float)I.n, I.has_lo ? 1 : 0};
-  k<<<grid, TG_THREADS, TGCfg<NCOL, 2>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, ktiles, nsplit, xstride, ep, I.err, limit,
+  k<<<grid, TG_THREADS, TGCfg<NCOL, 2>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, big, ktiles, nsplit, xstride, ep, I.err, limit,
                                                    run_flag);
   return cudaGetLastError();
 }

@@ -30,7 +30,9 @@ template <int NCOL, int MT = 1> struct TGCfg {
   static constexpr int A_BYTES = MT * A1_BYTES;
   static constexpr int X_BYTES = NCOL * TG_BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + X_BYTES;
-  static constexpr int STAGES = (200 * 1024) / STAGE_BYTES > 8 ? 8 : (200 * 1024) / STAGE_BYTES;
+  // as many stages as 225 KB of the 227 KB per CTA hold (at most 8): the bytes in flight hide
+  // the latency of the operand loads
+  static constexpr int STAGES = (225 * 1024) / STAGE_BYTES > 8 ? 8 : (225 * 1024) / STAGE_BYTES;
   static constexpr int ACC_COLS = MT * NCOL < 32 ? 32 : MT * NCOL;  // one accumulator (all row tiles)
   static constexpr int NACC = 2 * ACC_COLS <= 512 ? 2 : 1;           // double-buffered when TMEM allows
   static constexpr int TMEM_COLS = ACC_COLS * NACC;
@@ -40,7 +42,10 @@ template <int NCOL, int MT = 1> struct TGCfg {
 };
 
 // Work units: (MT row tiles of 128, column block); column block sp covers X rows
-// sp * xstride .. + NCOL; mtiles counts units of MT * 128 rows.  Epilogue interface:
+// sp * xstride .. + NCOL; mtiles counts groups of MT * 128 rows.  The first big_tiles groups
+// run as units of MT row tiles; the rest run one row tile per unit, so that the last wave of
+// a persistent grid holds units of half the work (a tail of one-tile units instead of a
+// partly filled wave of MT-tile units).  Epilogue interface:
 // Epi::row(taddr, row, m0, sp) is called by
 // every thread of warps 1-4 with taddr = TMEM address of this thread's accumulator row
 // (lane field set, column 0).  With NCOL <= 256 the accumulator is double-buffered in TMEM,
@@ -48,7 +53,7 @@ template <int NCOL, int MT = 1> struct TGCfg {
 template <int NCOL, class Epi, int MT = 1>
 __global__ void __launch_bounds__(TG_THREADS, 1)
     k_tensor_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int mtiles,
-                  int ktiles, int nsplit, int xstride, Epi epi, int* err, unsigned long long limit_ns,
+                  int big_tiles, int ktiles, int nsplit, int xstride, Epi epi, int* err, unsigned long long limit_ns,
                   const int* run_flag) {
   using C = TGCfg<NCOL, MT>;
   if (run_flag && *run_flag == 0) return;  // nothing to compute (every column inactive)
@@ -61,7 +66,21 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
   uint64_t* accempty = accfull + 2;          // [2] epilogue of a unit done (4 warp arrivals)
   uint32_t* tmem_slot = (uint32_t*)(accempty + 2);
   volatile int* sabort = (volatile int*)(tmem_slot + 1);
-  const int units = mtiles * nsplit;
+  const int nbig = big_tiles * nsplit;
+  const int units = nbig + (mtiles - big_tiles) * MT * nsplit;
+  // unit u -> first row tile, row tiles in the unit, column block
+  auto decode = [&](int u, int& rt0, int& mtu, int& sp) {
+    if (u < nbig) {
+      rt0 = (u / nsplit) * MT;
+      mtu = MT;
+      sp = u % nsplit;
+    } else {
+      const int v = u - nbig;
+      rt0 = big_tiles * MT + v / nsplit;
+      mtu = 1;
+      sp = v % nsplit;
+    }
+  };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -92,17 +111,19 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
       uint32_t ph = 0;
       long long issued = 0;
       for (int u = blockIdx.x; u < units && !*sabort; u += gridDim.x) {
-        const int tile = u / nsplit, xr0 = (u % nsplit) * xstride;
+        int rt0, mtu, sp;
+        decode(u, rt0, mtu, sp);
+        const int xr0 = sp * xstride;
         for (int kt = 0; kt < ktiles; ++kt) {
           if (!umma::mbar_wait(&empty[s], ph ^ 1, limit_ns, sabort)) {
             *sabort = 1;
             break;
           }
           unsigned char* st = smem + s * C::STAGE_BYTES;
-          umma::mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
+          umma::mbar_arrive_expect_tx(&full[s], mtu * C::A1_BYTES + C::X_BYTES);
 #pragma unroll
           for (int mt = 0; mt < MT; ++mt)
-            umma::tma_load_2d(st + mt * C::A1_BYTES, &tmA, &full[s], kt * TG_BK, (tile * MT + mt) * TG_BM);
+            if (mt < mtu) umma::tma_load_2d(st + mt * C::A1_BYTES, &tmA, &full[s], kt * TG_BK, (rt0 + mt) * TG_BM);
 #pragma unroll
           for (int h = 0; h < (NCOL + 255) / 256; ++h)
             umma::tma_load_2d(st + C::A_BYTES + h * 256 * TG_ROWB, &tmX, &full[s], kt * TG_BK, xr0 + h * 256);
@@ -127,6 +148,8 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
       uint32_t ph = 0;
       uint32_t it = 0;
       for (int u = blockIdx.x; u < units && !*sabort; u += gridDim.x, ++it) {
+        int rt0, mtu, sp;
+        decode(u, rt0, mtu, sp);
         const uint32_t buf = it % C::NACC, use = it / C::NACC;  // accumulator and its use count
         const uint32_t tacc = tmem + buf * C::ACC_COLS;
         // the accumulator must have been read out by the epilogue of its previous use
@@ -147,6 +170,7 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
           for (int kk = 0; kk < TG_BK / 16; ++kk) {
 #pragma unroll
             for (int mt = 0; mt < MT; ++mt) {
+              if (mt >= mtu) break;
               const uint64_t ad = umma::sw64_desc(a0 + mt * C::A1_BYTES + kk * 32);
 #pragma unroll
               for (int h = 0; h < C::NH; ++h) {
@@ -175,10 +199,11 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
       }
       umma::tc_fence_after();
       const int row = q * 32 + lane;
+      int rt0, mtu, sp;
+      decode(u, rt0, mtu, sp);
 #pragma unroll 1
-      for (int mt = 0; mt < MT; ++mt)
-        epi.row(tmem + buf * C::ACC_COLS + mt * NCOL + ((uint32_t)(q * 32) << 16), row,
-                ((u / nsplit) * MT + mt) * TG_BM, u % nsplit);
+      for (int mt = 0; mt < mtu; ++mt)
+        epi.row(tmem + buf * C::ACC_COLS + mt * NCOL + ((uint32_t)(q * 32) << 16), row, (rt0 + mt) * TG_BM, sp);
       umma::tc_fence_before();
       __syncwarp();
       if (lane == 0) umma::mbar_arrive(&accempty[buf]);

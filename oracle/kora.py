@@ -59,6 +59,11 @@ def lib():
         L.kora_set_threads.argtypes = [ctypes.c_int32]
         L.kora_max_threads.restype = ctypes.c_int32
         L.kora_philox4x32_10.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.kora_model_create.restype = ctypes.c_void_p
+        L.kora_model_create.argtypes = [ctypes.POINTER(_Spec), dp, dp]
+        L.kora_model_run.restype = ctypes.c_void_p
+        L.kora_model_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Spec), dp]
+        L.kora_model_free.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -134,7 +139,44 @@ def run(theta0, omega, *, k=5, c1=3.0, adj=None, onthefly=False, seed=1, fp64=Tr
     s = _spec(n, k, c1, onthefly, seed, fp64, t0, t1, dt, h0, atol, rtol, fixed, dense, initial_record, threads,
               max_attempts)
     L = lib()
-    r = L.kora_run(ctypes.byref(s), _dptr(theta0), _dptr(omega), _dptr(a))
+    return _result(L, L.kora_run(ctypes.byref(s), _dptr(theta0), _dptr(omega), _dptr(a)), n)
+
+
+class Model:
+    """A network kept between runs: its adjacency (dense, built once: 4 N^2 bytes in float for a
+    large N) or rank-K factor, and its frequencies.  ``run`` integrates one trajectory from theta0
+    with the given coupling constant and horizon, as ``run()`` above does."""
+
+    def __init__(self, omega, *, k=5, adj=None, onthefly=False, seed=1, fp64=True, threads=0):
+        omega = np.ascontiguousarray(omega, np.float64)
+        self.n = omega.size
+        a = None if adj is None else np.ascontiguousarray(adj, np.float64)
+        self.base = dict(k=k, onthefly=onthefly, seed=seed, fp64=fp64, threads=threads)
+        s = _spec(self.n, k, 0.0, onthefly, seed, fp64, 0.0, 1.0, 1.0, None, 1e-6, 0.0, False, 0, True, threads, None)
+        self.h = lib().kora_model_create(ctypes.byref(s), _dptr(omega), _dptr(a))
+
+    def run(self, theta0, *, c1=3.0, t0=0.0, t1=100.0, dt=1.0, h0=None, atol=1e-6, rtol=0.0, fixed=False, dense=0,
+            initial_record=True, max_attempts=None):
+        theta0 = np.ascontiguousarray(theta0, np.float64)
+        b = self.base
+        s = _spec(self.n, b["k"], c1, b["onthefly"], b["seed"], b["fp64"], t0, t1, dt, h0, atol, rtol, fixed, dense,
+                  initial_record, b["threads"], max_attempts)
+        L = lib()
+        return _result(L, L.kora_model_run(self.h, ctypes.byref(s), _dptr(theta0)), self.n)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().kora_model_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _result(L, r, n):
     try:
         def get(which):
             m = L.kora_result_size(r, which)

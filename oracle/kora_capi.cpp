@@ -3,6 +3,7 @@
 // Loaded with ctypes by tests/, __graft_entry__.smoke() and bench.py's CPU legs.
 // Nothing in the product links or loads it.  See kora_core.hpp for the
 // reference file:line each piece restates.
+#include <type_traits>
 #include "kora_core.hpp"
 
 typedef struct kora_spec {
@@ -118,6 +119,46 @@ void* kora_run(const kora_spec* s, const double* theta0, const double* omega, co
   if (s->fp64) go(double()); else go(float());
   return O;
 }
+
+// A model kept between runs (the dense adjacency of a large network is built once): runs of
+// several trajectories, or several samples of one, on the same network and frequencies.
+struct kora_model {
+  int fp64 = 0;
+  kora::Model<float> Mf;
+  kora::Model<double> Md;
+  std::vector<float> Af;
+  std::vector<double> Ad;
+};
+
+void* kora_model_create(const kora_spec* s, const double* omega, const double* adj) {
+  if (s->threads > 0) kora_set_threads(s->threads);
+  auto* m = new kora_model();
+  m->fp64 = s->fp64;
+  if (s->fp64) setup_model<double>(m->Md, m->Ad, s, omega, adj, s->c1);
+  else setup_model<float>(m->Mf, m->Af, s, omega, adj, s->c1);
+  return m;
+}
+
+// One run of the kept model from theta0 with the spec's coupling constant and horizon.
+void* kora_model_run(void* model, const kora_spec* s, const double* theta0) {
+  auto* m = (kora_model*)model;
+  kora::RunSpec S;
+  S.t0 = s->t0; S.t1 = s->t1; S.dt = s->dt; S.h0 = s->h0; S.atol = s->atol; S.rtol = s->rtol;
+  S.fixed = s->fixed; S.dense = s->dense; S.initial_record = s->initial_record; S.max_attempts = s->max_attempts;
+  if (s->threads > 0) kora_set_threads(s->threads);
+  auto* O = new kora::Outputs();
+  auto go = [&](auto& M) {
+    using R = typename std::remove_reference<decltype(M)>::type::value_type;
+    M.c1 = (R)s->c1;
+    std::vector<R> th((size_t)s->n);
+    for (int64_t i = 0; i < s->n; ++i) th[(size_t)i] = (R)theta0[i];
+    kora::run<R>(M, th.data(), S, *O);
+  };
+  if (m->fp64) go(m->Md); else go(m->Mf);
+  return O;
+}
+
+void kora_model_free(void* model) { delete (kora_model*)model; }
 
 static const std::vector<double>* pick(kora::Outputs* O, int which) {
   switch (which) {

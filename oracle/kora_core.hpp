@@ -188,6 +188,7 @@ double chunked_sum(int64_t n, F f) {
 
 // ---------------------------------------------------------------- model
 template <typename R> struct Model {
+  using value_type = R;
   int64_t N = 0;
   int32_t K = 0;
   int onthefly = 0;            // -A

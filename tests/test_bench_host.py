@@ -57,6 +57,10 @@ def test_tensor_roofline_counts_algorithmic_flops_per_gemm_launch():
     assert abs(r["achieved"] - round(flops / 2.9e-3 / 1e12, 1)) < 0.051
     assert r["issued_flops_per_launch"] == 2 * r["flops_per_launch"] == 2 * flops
     assert abs(r["whole_step_tflops"] - round(24.0 * n * 128 * 70 * n / 1.5 / 1e12, 1)) < 0.051
+    # a batch of 8 (padded to 16 columns) reads the same adjacency for 1/16 of the flops: HBM-bound
+    r8 = bench.roofline_tensor(n, 8, d, step_ms=1500.0)
+    assert r8["bound"] == "hbm" and r8["unit"] == "GB/s"
+    assert abs(r8["achieved"] - round(2.0 * n * n / 2.9e-3 / 1e9, 1)) < 0.051
 
 
 def test_window_inputs_share_trajectory_zero():

@@ -1,0 +1,95 @@
+"""The GPU path against the reference programs themselves.
+
+oracle/_ref holds the reference's own ``kuramoto`` (FP32) and ``kuramoto_64`` (FP64), built from
+its sources by oracle/build_ref.py: the checker.  Every program reads the same inputs through
+the reference's -R reload path (kuramoto.cu:466-521, 557-566; kuramoto_64.cu:472, 511, 560):
+fs.dat = theta0, t = 0, h = dt/100 (the first step of a fresh start, kuramoto.cu:459-463),
+frequencies.dat and, for the dense coupling, adj.dat.  They are float32 for ``kuramoto`` and
+for this project's drop-in CLI, and the same values widened exactly to float64 for
+``kuramoto_64``.
+
+The contract for the FP32 path, against ``kuramoto_64``:
+  * phases (thetas.dat) within 1e-4 rad for t <= 10, plus one float32 ulp of the stored phase.
+    thetas.dat is float32, and a Cauchy oscillator with |omega| ~ 1e3 reaches |theta| ~ 1e4 by
+    t = 10, where one ulp is 1e-3;
+  * the time average of r (order.dat) within 1e-3 over the whole horizon.
+The CPU oracle's FP64 restatement is pinned to ``kuramoto_64`` with the same bounds; it runs
+the coupling in its rank-K form, the same matrix as the stored adjacency (which holds it rounded
+to float32, a relative 6e-8).
+"""
+import os
+import shutil
+import tempfile
+
+import numpy as np
+import pytest
+
+import refprog as rp
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ref():
+    from oracle import build_ref
+    if not build_ref.prepared():
+        pytest.skip("oracle/_ref holds no prepared reference build (the reference sources were not available)")
+    if not build_ref.available():
+        build_ref.finish()
+    assert build_ref.available(), "the reference programs did not build"
+    return build_ref
+
+
+@pytest.fixture
+def workdir():
+    # the reference rewrites fs.dat after every accepted step: keep the files in memory
+    root = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    d = tempfile.mkdtemp(prefix="kura_ref_", dir=root)
+    yield d
+    shutil.rmtree(d, ignore_errors=True)
+
+
+def run_all(programs, workdir, n, theta0, omega, adj, **kw):
+    out = {}
+    for name, (exe, fp64) in programs.items():
+        d = os.path.join(workdir, name)
+        os.makedirs(d, exist_ok=True)
+        base = os.path.join(d, "run")
+        rp.write_inputs(base, theta0, omega, adj, 0.0, kw["dt"] / 100, fp64)
+        out[name] = rp.run(exe, base, n, fp64=fp64, **kw)
+    return out
+
+
+def check_against_fp64(o, r64, dt, label, t_phase=10.0):
+    m = r64.order.size
+    assert o.order.size == m, (label, o.order.size, m)
+    rows = int(round(t_phase / dt))
+    w = rp.wrapped(o.thetas[:rows], r64.thetas[:rows])
+    bound = 1e-4 + rp.ulp32(r64.thetas[:rows])
+    worst = np.unravel_index(np.argmax(w - bound), w.shape)
+    assert np.all(w <= bound), (label, "phase", float(w[worst]), float(bound[worst]), worst)
+    dmean = abs(float(np.mean(o.order, dtype=np.float64)) - float(np.mean(r64.order, dtype=np.float64)))
+    assert dmean <= 1e-3, (label, "mean r", dmean)
+    return float(np.max(w)), dmean, float(np.max(np.abs(o.order.astype(np.float64) - r64.order)))
+
+
+def test_config1_dense_against_reference_programs(native, oracle_lib, ref, workdir):
+    """The reference defaults as BASELINE config 1 sets them: N=5000, K=5 volcano adjacency
+    (seed 1), Cauchy omega of scale 1 (glibc rand, seed 1), theta0 = 0, c = 3, t = 100, dt = 1."""
+    n = 5000
+    th, om = oracle_lib.host_random_inputs(1, n, 0.0, 1.0, False)
+    adj = oracle_lib.volcano_adjacency(1, n, 5)
+    progs = {"gpu": (native.cli_path(), False), "kuramoto_64": (ref.binary(True), True)}
+    out = run_all(progs, workdir, n, th, om, adj, k=5, c=3.0, t1=100.0, dt=1.0, dense=1)
+    r64 = out["kuramoto_64"]
+    assert r64.order.size == 100 and r64.steps > 0
+    check_against_fp64(out["gpu"], r64, 1.0, "gpu")
+    check_against_fp64(oracle_as_reload(oracle_lib, th, om, k=5, c=3.0, onthefly=True, seed=1, t1=100.0,
+                                        dt=1.0), r64, 1.0, "oracle_64")
+
+
+def oracle_as_reload(oracle_lib, th, om, **kw):
+    """The FP64 oracle's records in the layout of a reload run (no t = 0 record)."""
+    r = oracle_lib.run(th, om, fp64=True, dense=1, initial_record=True, **kw)
+    return rp.Outputs(order=r.order[1:], thetas=r.thetas[1:], times=None, fs=None, steps=r.steps, wall_s=0.0,
+                      stdout="")
