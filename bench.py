@@ -52,22 +52,21 @@ WORKLOADS = {
                          atol=1e-6, rtol=0.0, shared_theta=False, adj_storage=1),
     # the shared-adjacency ensemble on tensor cores: N=65536, K=5 dense volcano adjacency,
     # 128 trajectories with distinct theta0 uniform in [0, 2pi), shared Cauchy omega, c=3,
-    # integrated toward t=20 with records every 0.01; one bench step is a window of 0.8 time
-    # units that continues the same integration (warm-up windows start it from t=0), so the
-    # default 5 warm-up and 20 timed steps cover t = 0..20.  The plain FP32 path
-    # (`dense65536w`) runs trajectory 0 of the same inputs beside it.
+    # integrated toward t=20 with records every 0.01; one bench step is 64 step attempts of every
+    # trajectory that continue the same integration (the warm-up steps start it from t=0).  The
+    # plain FP32 path (`dense65536w`) runs trajectory 0 of the same inputs beside it.
     "ensemble65536": dict(kind="windows", n=65536, k=5, cs=[3.0] * 128, init=2 * np.pi, t1=20.0, dt=0.01,
-                          window=0.8, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
-    "dense65536w": dict(kind="windows", n=65536, k=5, cs=[3.0], init=2 * np.pi, t1=20.0, dt=0.01, window=0.8,
+                          attempts=64, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
+    "dense65536w": dict(kind="windows", n=65536, k=5, cs=[3.0], init=2 * np.pi, t1=20.0, dt=0.01, attempts=64,
                         atol=1e-6, rtol=0.0, engine="persistent"),
     # the same ensemble at N=32768 (a 2.1 GB BF16 adjacency, larger than L2): profiling captures
     "ensemble32768": dict(kind="windows", n=32768, k=5, cs=[3.0] * 128, init=2 * np.pi, t1=20.0, dt=0.01,
-                          window=0.8, atol=1e-6, rtol=0.0, engine="tensor"),
+                          attempts=192, atol=1e-6, rtol=0.0, engine="tensor"),
     # a batch of 8 on either engine (the choice KURA_ENGINE_AUTO makes for small dense batches)
     "ensemble65536x8": dict(kind="windows", n=65536, k=5, cs=[3.0] * 8, init=2 * np.pi, t1=20.0, dt=0.01,
-                            window=0.8, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
+                            attempts=128, atol=1e-6, rtol=0.0, engine="tensor", plain="dense65536w"),
     "dense65536x8w": dict(kind="windows", n=65536, k=5, cs=[3.0] * 8, init=2 * np.pi, t1=20.0, dt=0.01,
-                          window=0.8, atol=1e-6, rtol=0.0, engine="persistent"),
+                          attempts=32, atol=1e-6, rtol=0.0, engine="persistent"),
     # the same ensemble at N=16384 (a 512 MiB BF16 adjacency, still larger than L2): profiling captures
     "ensemble16384": dict(n=16384, k=5, coupling=0, cs=[3.0] * 128, normal=False, init=2 * np.pi, t1=0.004,
                           dt=0.001, atol=1e-6, rtol=0.0, shared_theta=False, engine="tensor"),
@@ -95,10 +94,14 @@ WORKLOADS = {
 STATE_BYTES = 150.0
 
 
-def inputs(w, seed):
-    import kuramoto_gb300 as kg
+def inputs(w, seed, host_rng=None):
+    """Frequencies from glibc rand of `seed` (libkura's generator, or the oracle's byte-identical
+    one for the reference arm, which loads no product library) and seeded theta0."""
+    if host_rng is None:
+        import kuramoto_gb300 as kg
+        host_rng = kg.random_inputs
     n = w["n"]
-    _, om = kg.random_inputs(seed, n, 0.0, 1.0, w["normal"], gen_theta=False)
+    _, om = host_rng(seed, n, 0.0, 1.0, w["normal"], gen_theta=False)
     rng = np.random.default_rng(seed)
     B = len(w["cs"])
     if w["shared_theta"]:
@@ -193,8 +196,10 @@ def run_native(args, w):
     thetas, om = inputs(w, seed)
     n, B = w["n"], len(w["cs"])
     stream = torch.cuda.current_stream()
+    eng = kg.ENGINE_TENSOR if w.get("engine") == "tensor" else kg.ENGINE_PERSISTENT
     net = kg.Network(n, k=w["k"], coupling=w["coupling"], batch=B, seed=seed, atol=w["atol"], rtol=w["rtol"],
-                     dense_level=0, device=local, stream=stream.cuda_stream, adj_storage=w.get("adj_storage", 0))
+                     dense_level=0, device=local, stream=stream.cuda_stream, adj_storage=w.get("adj_storage", 0),
+                     engine=eng)
     net.set_frequencies(om)
     if w["coupling"] == 0:
         net.generate_adjacency()
@@ -573,14 +578,29 @@ def main_surrogate(args, w):
         print(json.dumps(line))
 
 
-def cpu_baseline(w, om, thetas, threads, sample_steps=None):
+# the CPU sample of a dense workload: about this many multiply-adds (12 N^2 per step attempt:
+# six RHS, two GEMV passes each), some 10-30 s of host time
+CPU_DENSE_MACS = 3e11
+
+
+def cpu_sample_attempts(w):
+    """None (the whole workload) for the regenerated coupling, whose CPU cost is O(N K) per RHS;
+    a bounded number of step attempts of the first trajectory for a dense adjacency."""
+    if w["coupling"] == 1:
+        return None
+    return max(1, int(CPU_DENSE_MACS / (12.0 * w["n"] * w["n"])))
+
+
+def cpu_baseline(w, om, thetas, threads):
     from oracle import kora
     n = w["n"]
+    att = cpu_sample_attempts(w)
+    cs = w["cs"] if att is None else w["cs"][:1]
     t0 = time.perf_counter()
     steps = 0
-    for b, c in enumerate(w["cs"]):
+    for b, c in enumerate(cs):
         r = kora.run(thetas[b], om, k=w["k"], c1=c, onthefly=w["coupling"] == 1, seed=1, fp64=False, t1=w["t1"],
-                     dt=w["dt"], atol=w["atol"], rtol=w["rtol"], threads=threads)
+                     dt=w["dt"], atol=w["atol"], rtol=w["rtol"], threads=threads, max_attempts=att)
         steps += r.steps
     el = time.perf_counter() - t0
     return steps * n / el, el, steps
@@ -647,9 +667,10 @@ def window_inputs(w, seed, host_rng):
 
 
 class Windowed:
-    """One integration toward t1 on one handle, advanced a window at a time: kura_set_horizon
-    after a finished kura_run continues every trajectory on the device (phases, FSAL slope and
-    step size kept), so the windows are consecutive pieces of one uninterrupted run."""
+    """One integration toward t1 on one handle, advanced a budget of step attempts at a time
+    (kura_advance): every trajectory keeps its phases, FSAL slope and step size on the device, so
+    the steps are consecutive pieces of one uninterrupted run, and every trajectory stays active
+    (no trajectory waits for the others at a step boundary)."""
 
     def __init__(self, w, thetas, om, seed, device, stream):
         import kuramoto_gb300 as kg
@@ -663,42 +684,46 @@ class Windowed:
         for b in range(self.B):
             self.net.set_coupling(b, w["cs"][b])
             self.net.set_state(b, thetas[b], 0.0, w["dt"] / 100)
-        self.t_end = 0.0
-        self.first = True
+        self.net.set_horizon(w["t1"], w["dt"], True)
+        self.running = self.B
         self.rec = [dict() for _ in range(self.B)]  # t_eval -> r
 
-    def horizon(self):
-        self.t_end += self.w["window"]
-        self.net.set_horizon(self.t_end, self.w["dt"], self.first)
-        self.first = False
-
-    def run(self):
+    def step(self):
         rec = self.rec
-        self.net.run(on_output=lambda b, i, te, r, th, cp: rec[b].__setitem__(round(te, 9), r) and False)
+        self.running = self.net.advance(self.w["attempts"], on_output=lambda b, i, te, r, th, cp:
+                                        rec[b].__setitem__(round(te, 9), r) and False)
+
+    def times(self):
+        return [self.net.state(b)[1] for b in range(self.B)]
 
     def close(self):
         self.net.close()
 
 
-def timed_windows(win, steps, stream, clocks=None):
-    """`steps` windows timed with CUDA events on the handle's stream; returns the accepted
-    oscillator-steps, the event time and the stats deltas."""
+def timed_windows(win, steps, stream):
+    """`steps` budgets of step attempts timed with CUDA events on the handle's stream (fewer when
+    every trajectory reaches t1 first); returns the accepted oscillator-steps, the event time, the
+    stats deltas and the steps taken."""
     import torch
     st0 = win.net.stats()
     ms = 0.0
+    done = 0
     for _ in range(steps):
-        win.horizon()
+        if win.running == 0:
+            break
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        win.run()
+        win.step()
         e1.record(stream)
         torch.cuda.synchronize()
         ms += e0.elapsed_time(e1)
+        done += 1
     st1 = win.net.stats()
     d = {k: st1[k] - st0[k] for k in ("accepted", "rejected", "launches", "kernel_ms", "coupling_ms",
                                      "coupling_launches")}
+    d["steps"] = done
     return d["accepted"] * win.n, ms, d
 
 
@@ -743,9 +768,9 @@ def main_windows(args, w):
               "engine": "tcgen05 split-BF16 ensemble" if w["engine"] == "tensor" else "plain FP32 persistent",
               "batch": B, "c": w["cs"][0], "theta0": "uniform [0, 2pi), one numpy stream per seed",
               "frequencies": "cauchy scale 1 (glibc rand, seed 1), shared", "t1": w["t1"], "dt": w["dt"],
-              "window": w["window"], "atol": w["atol"], "rtol": w["rtol"],
-              "step": "one window of %g time units continuing the same integration toward t1; warm-up windows "
-                      "start it from t=0" % w["window"],
+              "atol": w["atol"], "rtol": w["rtol"],
+              "step": "%d step attempts of every trajectory (kura_advance) continuing one integration toward "
+                      "t1; the warm-up steps start it from t=0" % w["attempts"],
               "l2": "inputs larger than L2 (the adjacency, %.1f GB, is streamed by every RHS); not flushed"
                     % (n * n * (2 if w["engine"] == "tensor" else 4) / 1e9),
               "parallelism": "replicas" if ws > 1 else "single"}
@@ -777,8 +802,9 @@ def main_windows(args, w):
                                   "d2h_bytes_per_step": 0}}))
         return
 
-    if args.until is not None:
-        args.steps = max(1, int(round(args.until / w["window"])) - args.warmup)
+    if args.until is not None:  # one whole integration to t1 = args.until, timed after the warm-up
+        w = dict(w, t1=args.until)
+        args.steps = 1 << 30
     import torch
     import kuramoto_gb300 as kg
     os.environ.setdefault("KURA_TIME_COUPLING", "1")
@@ -797,18 +823,19 @@ def main_windows(args, w):
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
-        win.horizon()
-        win.run()
+        win.step()
     barrier()
     with Clocks(local) as clk:
         units, ms, d = timed_windows(win, args.steps, stream)
         barrier()
+    steps = d["steps"]
     units_all, ms_max = combine_ranks(units, ms, "cuda")
     value = units_all / (ms_max / 1e3)
-    t_value_end = win.t_end
+    t_reached = win.times()
 
-    # ---- e2e: the same windows through host buffers (frequencies and every trajectory's phases
-    # copied in from pinned memory with their own t and h; records and phases copied out)
+    # ---- e2e: further steps through host buffers: the frequencies and every trajectory's phases
+    # copied in from pinned memory with their own t and h (as a -R resume through fs.dat), the
+    # budget of attempts, then the records and the phases copied out
     om_pin = pinned(om)
     th_pin = [pinned(np.zeros(n, np.float32)) for _ in range(B)]
     th_t = [0.0] * B
@@ -817,15 +844,16 @@ def main_windows(args, w):
         _, th_t[b], th_h[b] = win.net.state(b, out=th_pin[b])
     e2e_units = e2e_s = 0.0
     h2d = d2h = 0
-    for it in range(0 if args.no_e2e else args.steps):
+    for it in range(0 if (args.no_e2e or args.until is not None) else steps):
+        if min(th_t) >= w["t1"]:
+            break
         barrier()
         t0 = time.perf_counter()
         win.net.set_frequencies(om_pin)
         for b in range(B):
             win.net.set_state(b, th_pin[b], th_t[b], th_h[b])
-        win.t_end += w["window"]
-        win.net.set_horizon(win.t_end, w["dt"], False)
-        win.net.run()
+        win.net.set_horizon(w["t1"], w["dt"], False)
+        win.net.advance(w["attempts"])
         rs = [win.net.order(b) for b in range(B)]
         for b in range(B):
             _, th_t[b], th_h[b] = win.net.state(b, out=th_pin[b])
@@ -841,41 +869,41 @@ def main_windows(args, w):
 
     # ---- the plain FP32 path on trajectory 0 of the same inputs
     plain = None
-    if w.get("plain"):
-        pw = dict(WORKLOADS[w["plain"]])
+    if w.get("plain") and args.until is None:
+        pw = dict(WORKLOADS[w["plain"]], t1=w["t1"])
         pwin = Windowed(pw, thetas[:1], om, seed, local, stream.cuda_stream)
         for _ in range(2):
-            pwin.horizon()
-            pwin.run()
+            pwin.step()
         pu, pms, pd = timed_windows(pwin, 2, stream)
         pwin.close()
         pval = pu / (pms / 1e3)
         pk = pd["kernel_ms"] / max(pd["launches"], 1)
         bytes_launch = 24.0 * n * pd["accepted"] * n / max(pd["launches"], 1)
-        plain = {"value": pval, "unit": "osc-steps/s", "windows": 2, "accepted_steps": pd["accepted"],
-                 "ratio_batched_over_plain": value / pval,
+        plain = {"value": pval, "unit": "osc-steps/s", "steps": pd["steps"], "attempts_per_step": pw["attempts"],
+                 "accepted_steps": pd["accepted"], "ratio_batched_over_plain": value / pval,
                  "roofline": roofline_hbm(bytes_launch, pk)}
     if rank != 0:
         return
-    line = {"metric": metric, "value": value, "unit": "osc-steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 state, bf16 split operands, f32 accumulation", "data": "synthetic",
-            "config": config}
+    line = {"metric": metric, "value": value, "unit": "osc-steps/s", "n_gpus": ws, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / max(steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 state, bf16 split operands, f32 accumulation",
+            "data": "synthetic", "config": config}
     line["e2e"] = {"value": e2e_value, "unit": "osc-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
     if w["engine"] == "tensor":
         # per attempt: coefficients, 6 x (stage phases, GEMM), error, decision, 2 output kernels;
-        # per window: the first slope's 6 kernels
-        line["gpu_launches"] = 17 * d["launches"] + 6 * args.steps
+        # per step: the first-slope kernels (their GEMM is skipped once the slopes are on the device)
+        line["gpu_launches"] = 17 * d["launches"] + 6 * steps
         line["roofline"] = roofline_tensor(n, B, d, ms)
     else:
-        # one persistent launch per window; A is read once per RHS for the whole batch
+        # one persistent launch per step; A is read once per RHS for the whole batch
         line["gpu_launches"] = d["launches"]
         line["roofline"] = roofline_hbm(24.0 * n * n * d["accepted"] / B / max(d["launches"], 1),
                                         d["kernel_ms"] / max(d["launches"], 1))
     line["clocks"] = clk.summary()
     line["accepted_steps"] = {"timed": d["accepted"], "rejected": d["rejected"],
-                              "per_trajectory_per_window": d["accepted"] / B / args.steps,
-                              "t_reached": round(t_value_end, 4)}
+                              "per_trajectory_per_step": d["accepted"] / B / max(steps, 1),
+                              "t_reached": {"min": round(min(t_reached), 4), "mean": round(float(np.mean(t_reached)), 4),
+                                            "max": round(max(t_reached), 4)}}
     if plain:
         line["plain_fp32"] = plain
     if not args.no_cpu:
@@ -887,16 +915,17 @@ def main_windows(args, w):
                                           "adjacency built once beforehand in %.1f s), float32 oracle restating the "
                                           "reference program, two GEMV passes per RHS, OpenMP"
                                           % (CPU_ATTEMPTS, st, el, build_s)}
+    if not args.no_cpu or args.until is not None:
         errs, cnt = [], 0
         for b in sorted({0, B // 2, B - 1}):
-            ref, _ = fp64_records(w, thetas[b], om, w["cs"][b], t_value_end, threads, seed)
+            ref, _ = fp64_records(w, thetas[b], om, w["cs"][b], t_reached[b], threads, seed)
             common = [t for t in rec[b] if t in ref]
             cnt += len(common)
             if common:
                 errs.append(max(abs(float(rec[b][t]) - float(ref[t])) for t in common))
         line["r_err_vs_fp64"] = max(errs) if errs else None
-        line["r_err_sample"] = ("trajectories %s, %d records at t <= %.3f against the FP64 oracle"
-                                % (sorted({0, B // 2, B - 1}), cnt, t_value_end))
+        line["r_err_sample"] = ("trajectories %s, %d records from t=0 to each one's time reached, against the "
+                                "FP64 oracle" % (sorted({0, B // 2, B - 1}), cnt))
     print(json.dumps(line))
 
 
@@ -988,8 +1017,7 @@ def main():
         if rank != 0:
             return
         from oracle import kora
-        import kuramoto_gb300 as kg  # host RNG only (glibc rand), no GPU use
-        thetas, om = inputs(w, 1)
+        thetas, om = inputs(w, 1, kora.host_random_inputs)
         for _ in range(args.warmup):
             cpu_baseline(w, om, thetas, threads)
         tot_units = 0.0
@@ -1004,8 +1032,11 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": value, "unit": "osc-steps/s", "cores": threads, "kind": "port",
-                                 "sample": "whole workload per step (%d trajectories to t=%g), float32 oracle "
-                                           "restating the reference program, OpenMP" % (B, w["t1"])},
+                                 "sample": ("whole workload per step (%d trajectories to t=%g)" % (B, w["t1"])
+                                            if cpu_sample_attempts(w) is None else
+                                            "trajectory 0, %d step attempts from t=0 per step"
+                                            % cpu_sample_attempts(w)) +
+                                           ", float32 oracle restating the reference program, OpenMP"},
                 "e2e": {"value": value, "unit": "osc-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -1025,9 +1056,12 @@ def main():
     line["accepted_steps_per_run"] = res["acc_per_step"]
     if not args.no_cpu:
         v, el, steps = cpu_baseline(w, res["om"], res["thetas"], threads)
+        att = cpu_sample_attempts(w)
         line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
-                                "sample": "whole workload (%d trajectories to t=%g, %d accepted steps, %.1f s), "
-                                          "float32 oracle restating the reference program" % (B, w["t1"], steps, el)}
+                                "sample": ("whole workload (%d trajectories to t=%g" % (B, w["t1"]) if att is None
+                                           else "trajectory 0, %d step attempts from t=0 (" % att) +
+                                          ", %d accepted steps, %.1f s), float32 oracle restating the reference "
+                                          "program" % (steps, el)}
         if w["coupling"] == 1:
             acc = volcano_accuracy(w, res["thetas"], res["om"], instance_seed(res["rank"]), 0, threads)
             line["accuracy"] = acc

@@ -36,8 +36,8 @@ extern "C" {
 #define KURA_COUPLING_DENSE 0   /* adjacency stored in HBM (reference default) */
 #define KURA_COUPLING_VOLCANO 1 /* rank-K volcano factor regenerated from Philox (reference -A) */
 
-/* KURA_ENGINE_AUTO picks the tensor-core ensemble for a dense network with batch > 8 and
- * the CUDA-core persistent kernel otherwise.  The persistent kernel takes batch <= 8 (dense
+/* KURA_ENGINE_AUTO picks the tensor-core ensemble for a dense network with batch > 8, or with
+ * batch >= 2 at dense level 0, and the CUDA-core persistent kernel otherwise.  The persistent kernel takes batch <= 8 (dense
  * or volcano coupling, every dense level); the tensor-core ensemble takes a dense network
  * with batch <= 128, keeps only the order parameter (dense level 0) and reports no per-step
  * records.  The reference has neither: it integrates one trajectory per process. */
@@ -132,6 +132,14 @@ int kura_set_horizon(kura_handle* h, double t1, double dt, int32_t initial_recor
 
 /* integrate every trajectory to t1 (dp45_run with step_eval, dp45.cu:148-164) */
 int kura_run(kura_handle* h, const kura_callbacks* cb);
+/* integrate for at most `attempts` step attempts of every unfinished trajectory (the tensor
+ * engine takes them in groups of four), then return with the state kept on the device;
+ * *running (may be NULL) receives the trajectories still short of t1.  A later kura_advance or
+ * kura_run continues exactly where this one stopped.  The reference's counterpart is a run cut
+ * short by its job's time limit and resumed with -R (job1.sh:3 ckpt partition; kuramoto.cu:466-494),
+ * here without losing the FSAL slope or the step size.  Records reach the observers as in
+ * kura_run. */
+int kura_advance(kura_handle* h, const kura_callbacks* cb, int64_t attempts, int32_t* running);
 
 /* current phases (unwrapped), time and step of one trajectory */
 int kura_get_state(kura_handle* h, int32_t traj, float* theta, double* t, double* step);

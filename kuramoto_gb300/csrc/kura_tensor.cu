@@ -794,7 +794,7 @@ static cudaError_t attempt(TensorEngine::Impl& I) {
   return cudaGetLastError();
 }
 
-int TensorEngine::run(std::vector<TrajG>& traj, kura_stats& stats) {
+int TensorEngine::run(std::vector<TrajG>& traj, kura_stats& stats, long long max_replays) {
   Impl& I = *d;
   if (!I.adj_set) { g_terr = "adjacency not set"; return KURA_ERR_INVALID; }
   TCU(cudaMemsetAsync(I.err, 0, sizeof(int), I.st));
@@ -843,6 +843,7 @@ int TensorEngine::run(std::vector<TrajG>& traj, kura_stats& stats) {
         }
       }
     }
+    if (max_replays > 0 && launches >= max_replays) break;
   }
   TCU(cudaEventRecord(I.ev1, I.st));
   TCU(cudaMemcpyAsync(traj.data(), I.traj, sizeof(TrajG) * I.B, cudaMemcpyDeviceToHost, I.st));

@@ -24,7 +24,9 @@ class TensorEngine {
   float* staging(int b);  // device buffer of n floats for trajectory b's uploads
   int set_state(int b, const float* theta_dev, const TrajG& T);
   int set_horizon(const std::vector<float>& t_eval, int ring, std::vector<TrajG>& traj);
-  int run(std::vector<TrajG>& traj, kura_stats& stats);
+  // integrates until every trajectory is done or, with max_replays > 0, after that many step
+  // attempts (rounded up to a multiple of four: the attempt graph is replayed four at a time)
+  int run(std::vector<TrajG>& traj, kura_stats& stats, long long max_replays = -1);
   int read_order(int b, int count, float* r, int* idx);  // records: r and output index (-1: t0)
   int get_state(int b, int rot_y, float* theta);
   int evaluate(int mode, int b, float* theta_out, float* coup_out);  // 1: end record, 2: RHS

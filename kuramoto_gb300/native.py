@@ -112,6 +112,7 @@ def lib():
         "kura_set_state_device": (i32, [P, i32, P, f64, f64]),
         "kura_set_horizon": (i32, [P, f64, f64, i32]),
         "kura_run": (i32, [P, ctypes.POINTER(Callbacks)]),
+        "kura_advance": (i32, [P, ctypes.POINTER(Callbacks), i64, ctypes.POINTER(i32)]),
         "kura_get_state": (i32, [P, i32, fp, ctypes.POINTER(f64), ctypes.POINTER(f64)]),
         "kura_get_order": (i32, [P, i32, fp, i64, ctypes.POINTER(i64)]),
         "kura_final_record": (i32, [P, i32, fp, fp, ctypes.POINTER(f64), ctypes.POINTER(f64)]),
@@ -243,6 +244,18 @@ class Network:
         """Integrate to the horizon.  Optional Python observers receive
         on_step(traj, t, h, step), on_output(traj, index, t_eval, r, theta, couplings)
         and on_chunk(traj, t, h, theta); arrays are copies."""
+        cb, keep = self._callbacks(on_step, on_output, on_chunk)
+        _check(lib().kura_run(self.h, ctypes.byref(cb) if keep else None))
+
+    def advance(self, attempts, on_step=None, on_output=None, on_chunk=None):
+        """At most ``attempts`` step attempts of every unfinished trajectory (kura_advance);
+        returns the number of trajectories still short of the horizon's end."""
+        cb, keep = self._callbacks(on_step, on_output, on_chunk)
+        running = ctypes.c_int32(0)
+        _check(lib().kura_advance(self.h, ctypes.byref(cb) if keep else None, int(attempts), ctypes.byref(running)))
+        return running.value
+
+    def _callbacks(self, on_step, on_output, on_chunk):
         n = self.n
         cb = Callbacks()
         keep = []
@@ -262,7 +275,8 @@ class Network:
             f = CHUNK_CB(lambda u, b, t, h, th: int(bool(on_chunk(b, t, h, np.ctypeslib.as_array(th, (n,)).copy()))))
             cb.on_chunk = f
             keep.append(f)
-        _check(lib().kura_run(self.h, ctypes.byref(cb) if keep else None))
+        self._keep = keep  # the C callbacks live until the next call
+        return cb, keep
 
     def state(self, traj=0, out=None):
         """(theta, t, h) of a trajectory; theta is written into ``out`` when given (a

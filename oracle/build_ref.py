@@ -17,7 +17,10 @@ and the GPU host may have another CPU architecture:
      CUDA runtime, cuBLAS and cuRAND into ``oracle/_ref/kuramoto`` and ``kuramoto_64``.
 
 ``_FORTIFY_SOURCE`` is undefined during preprocessing so that the intermediates carry no
-glibc inline wrappers specific to the preprocessing host.
+glibc inline wrappers specific to the preprocessing host.  The host compile uses
+``-fsigned-char``: the reference stores getopt's int result in a ``char`` and compares it with
+-1 (kuramoto.cu:292, 299), which terminates its option loop only where char is signed (x86_64);
+with aarch64's unsigned char the loop never ends.
 """
 import os
 import shutil
@@ -96,7 +99,7 @@ def finish():
         for s in srcs:
             o = os.path.join(OUT, s + ".o")
             objs[s] = o
-            jobs.append(["g++", "-O3", "-w", "-c", "-x", "c++-cpp-output", _intermediate(s), "-o", o])
+            jobs.append(["g++", "-O3", "-w", "-fsigned-char", "-c", "-x", "c++-cpp-output", _intermediate(s), "-o", o])
     with ThreadPoolExecutor(len(jobs)) as ex:
         list(ex.map(_run, jobs))
     for name, srcs in PROGRAMS.items():

@@ -87,3 +87,39 @@ def test_horizon_needs_fresh_or_finished_trajectories(native):
     net.set_horizon(2.0, 0.5, False)
     net.run()
     net.close()
+
+
+@pytest.mark.parametrize("coupling,engine,batch,chunk", [(VOLCANO, PERSISTENT, 3, 17), (DENSE, TENSOR, 16, 12)])
+def test_advance_in_chunks_equals_one_run(native, coupling, engine, batch, chunk):
+    """kura_advance: a run cut into budgets of step attempts takes the steps of one run and
+    delivers the same records, with every trajectory active until it reaches the end."""
+    n = 600
+    _, om = normal_inputs(n, 9)
+    thetas = [normal_inputs(n, 60 + b, init=2 * np.pi)[0] for b in range(batch)]
+    cs = [1.5 + 0.5 * (b % 5) for b in range(batch)]
+
+    one = _net(native, n, coupling, engine, thetas, om, cs)
+    one.set_horizon(5.0, 0.25, True)
+    rec1 = {b: [] for b in range(batch)}
+    _records(one, batch, rec1)
+    st1 = one.stats()
+    fin1 = [one.state(b) for b in range(batch)]
+    one.close()
+
+    cut = _net(native, n, coupling, engine, thetas, om, cs)
+    cut.set_horizon(5.0, 0.25, True)
+    rec2 = {b: [] for b in range(batch)}
+    calls, running = 0, batch
+    while running:
+        running = cut.advance(chunk, on_output=lambda b, i, te, r, th, cp: rec2[b].append((round(te, 9), r)) and False)
+        calls += 1
+        assert calls < 10000
+    st2 = cut.stats()
+    fin2 = [cut.state(b) for b in range(batch)]
+    cut.close()
+
+    assert calls > 3
+    assert st1["accepted"] == st2["accepted"] and st1["rejected"] == st2["rejected"]
+    for b in range(batch):
+        assert rec1[b] == rec2[b], b
+        assert fin1[b][1] == fin2[b][1] and np.array_equal(fin1[b][0], fin2[b][0])

@@ -21,9 +21,9 @@ def f32_ulp(x):
 
 
 def make(native, n, k, coupling, theta, omega, c=3.0, batch=1, seed=1, dense_level=1, atol=1e-6, rtol=0.0,
-         fixed=False, t1=10.0, dt=1.0, h0=None, adj=None, thetas=None, cs=None):
+         fixed=False, t1=10.0, dt=1.0, h0=None, adj=None, thetas=None, cs=None, engine=1):
     net = native.Network(n, k=k, coupling=coupling, batch=batch, seed=seed, atol=atol, rtol=rtol, fixed_step=fixed,
-                         dense_level=dense_level)
+                         dense_level=dense_level, engine=engine)
     net.set_frequencies(omega)
     if coupling == DENSE:
         if adj is None:

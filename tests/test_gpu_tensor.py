@@ -112,3 +112,20 @@ def test_tensor_rejects_unsupported(native):
         native.Network(100, k=5, coupling=1, batch=16, engine=TENSOR)  # volcano coupling
     with pytest.raises(native.KuraError):
         native.Network(100, k=5, coupling=DENSE, batch=16, engine=TENSOR, dense_level=1)
+
+
+def test_auto_engine_choice(native):
+    """KURA_ENGINE_AUTO: the tensor engine (it reports grid 0) for a dense batch of two or more
+    that keeps only r, and for any dense batch above 8; the persistent kernel for one trajectory,
+    for per-step records (dense level >= 1), for the int8 adjacency and for the -A coupling."""
+    def grid(**kw):
+        net = native.Network(300, k=5, **kw)
+        g = net.stats()["grid"]
+        net.close()
+        return g
+    assert grid(coupling=DENSE, batch=2, dense_level=0) == 0
+    assert grid(coupling=DENSE, batch=16, dense_level=0) == 0
+    assert grid(coupling=DENSE, batch=1, dense_level=0) > 0
+    assert grid(coupling=DENSE, batch=4, dense_level=1) > 0
+    assert grid(coupling=DENSE, batch=4, dense_level=0, adj_storage=native.ADJ_I8) > 0
+    assert grid(coupling=1, batch=4, dense_level=0) > 0
