@@ -39,7 +39,7 @@ WORKLOADS = {
                         t1=50.0, dt=1.0, atol=1e-6, rtol=0.0, shared_theta=True),
     # the reference's default dense case (configs: N=5000, K=5, c=3, Cauchy, theta0=0, t=100, dt=1)
     "dense5000": dict(n=5000, k=5, coupling=0, cs=[3.0], normal=False, init=0.0, t1=100.0, dt=1.0, atol=1e-6,
-                      rtol=0.0, shared_theta=True),
+                      rtol=0.0, shared_theta=True, fresh=True),
     # the plain FP32 path at N=65536 (17.2 GB adjacency read once per RHS; x8: shared by 8
     # trajectories of one pass), Cauchy omega, theta0 uniform in [0, 2pi); the Cauchy
     # outliers of N=65536 force steps of ~1e-4, so the horizon is short
@@ -101,7 +101,9 @@ def inputs(w, seed, host_rng=None):
         import kuramoto_gb300 as kg
         host_rng = kg.random_inputs
     n = w["n"]
-    _, om = host_rng(seed, n, 0.0, 1.0, w["normal"], gen_theta=False)
+    # a fresh start draws N values for theta0 before the frequencies (kuramoto.cu:498-541); a run
+    # whose phases come from a file through -R draws only the frequencies
+    _, om = host_rng(seed, n, 0.0, 1.0, w["normal"], gen_theta=bool(w.get("fresh")))
     rng = np.random.default_rng(seed)
     B = len(w["cs"])
     if w["shared_theta"]:
@@ -1058,9 +1060,9 @@ def main():
         v, el, steps = cpu_baseline(w, res["om"], res["thetas"], threads)
         att = cpu_sample_attempts(w)
         line["cpu_baseline"] = {"value": v, "unit": "osc-steps/s", "cores": threads, "kind": "port",
-                                "sample": ("whole workload (%d trajectories to t=%g" % (B, w["t1"]) if att is None
+                                "sample": ("whole workload (%d trajectories to t=%g, " % (B, w["t1"]) if att is None
                                            else "trajectory 0, %d step attempts from t=0 (" % att) +
-                                          ", %d accepted steps, %.1f s), float32 oracle restating the reference "
+                                          "%d accepted steps, %.1f s), float32 oracle restating the reference "
                                           "program" % (steps, el)}
         if w["coupling"] == 1:
             acc = volcano_accuracy(w, res["thetas"], res["om"], instance_seed(res["rank"]), 0, threads)

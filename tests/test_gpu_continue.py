@@ -89,7 +89,7 @@ def test_horizon_needs_fresh_or_finished_trajectories(native):
     net.close()
 
 
-@pytest.mark.parametrize("coupling,engine,batch,chunk", [(VOLCANO, PERSISTENT, 3, 17), (DENSE, TENSOR, 16, 12)])
+@pytest.mark.parametrize("coupling,engine,batch,chunk", [(VOLCANO, PERSISTENT, 3, 5), (DENSE, TENSOR, 16, 4)])
 def test_advance_in_chunks_equals_one_run(native, coupling, engine, batch, chunk):
     """kura_advance: a run cut into budgets of step attempts takes the steps of one run and
     delivers the same records, with every trajectory active until it reaches the end."""
