@@ -246,6 +246,7 @@ def run_native(args, w):
     acc_per_step = st1["accepted"]
     launches = st1["launches"] - st0["launches"]
     kernel_ms = st1["kernel_ms"] - st0["kernel_ms"]
+    barriers = st1["barriers"] - st0["barriers"]
     units, ms = combine_ranks(acc_per_step * n * args.steps, ms, "cuda")
     value = units / (ms / 1e3)
     orders = [net.order(b) for b in range(B)]
@@ -281,6 +282,7 @@ def run_native(args, w):
     e2e_value = e2e_units / (e2e_ms / 1e3)
     net.close()
     res = dict(value=value, ms=ms, wall=t_wall, kernel_ms=kernel_ms, launches=launches, acc_per_step=acc_per_step,
+               barriers=barriers,
                e2e_value=e2e_value, h2d=h2d, d2h=d2h, clocks=clk.summary(), orders=orders, thetas=thetas, om=om,
                rank=rank, ws=ws, B=B)
     return res
@@ -326,9 +328,19 @@ def roofline(w, res, args):
             traffic = t["bytes_per_accepted_osc_step"] * acc_per_launch * n
     except Exception:
         pass
-    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": src,
-            "bytes_per_unit": per_unit, "kernel_ms_per_launch": round(kernel_s * 1e3, 3)}
+    out = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+           "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": src,
+           "bytes_per_unit": per_unit, "kernel_ms_per_launch": round(kernel_s * 1e3, 3)}
+    if w["coupling"] == 1 and res.get("barriers"):
+        # the DP45 state of this workload stays in L2, so DRAM does not bind it: every coupling
+        # evaluation and every error norm is one grid barrier, and the time between barriers
+        # (phase A, the gather, phase C at one CTA per SM) is what the kernel costs
+        out["binding"] = {"kind": "latency: one grid barrier per coupling evaluation and per error norm",
+                          "us_per_barrier_interval": round(res["kernel_ms"] * 1e3 / res["barriers"], 2),
+                          "barriers_per_accepted_step": round(res["barriers"] / max(acc_per_launch *
+                                                                                     res["launches"] /
+                                                                                     len(w["cs"]), 1), 2)}
+    return out
 
 
 def multi_inputs(w, seed):

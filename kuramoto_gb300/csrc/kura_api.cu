@@ -656,9 +656,19 @@ extern "C" int kura_run(kura_handle* h, const kura_callbacks* cb) {
     h->stats.accepted = acc;
     h->stats.rejected = rej;
     if (errc) {
-      const char* m = errc == KURA_ERR_STEP_UNDERFLOW ? "step size underflow"
+      std::string m = errc == KURA_ERR_STEP_UNDERFLOW ? "step size underflow"
                       : errc == KURA_ERR_UNSUPPORTED ? "more than 32 output times crossed in one step"
                                                       : "non-finite error norm";
+      for (int b = 0; b < h->B; ++b) {
+        const TrajG& T = h->htraj[b];
+        if (T.status == errc) {
+          char buf[200];
+          snprintf(buf, sizeof buf, " (trajectory %d: t %.9g, h %.3g, t_last %.9g, outputs %d..%d of %d)", b, T.t,
+                   T.h, T.t_last, T.eval_i, T.eval_end, h->n_eval);
+          m += buf;
+          break;
+        }
+      }
       return fail(errc, m);
     }
     for (int b = 0; b < h->B; ++b) h->finished[b] = h->htraj[b].status == 1;

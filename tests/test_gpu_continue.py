@@ -123,3 +123,29 @@ def test_advance_in_chunks_equals_one_run(native, coupling, engine, batch, chunk
     for b in range(batch):
         assert rec1[b] == rec2[b], b
         assert fin1[b][1] == fin2[b][1] and np.array_equal(fin1[b][0], fin2[b][0])
+
+
+def test_resume_through_host_state_on_the_tensor_engine(native):
+    """The pattern of a -R resume per budget: read every trajectory's phases, t and h to the
+    host, set them back (each with its own t and h), set the horizon and advance again.  The
+    Cauchy frequencies give oscillators with |omega| in the hundreds, so the phases grow large
+    and the trajectories' times spread apart."""
+    from helpers import cauchy_inputs
+    n, batch = 2000, 16
+    _, om = cauchy_inputs(n, 5)
+    thetas = [cauchy_inputs(n, 70 + b)[0] for b in range(batch)]
+    net = _net(native, n, DENSE, TENSOR, thetas, om, [3.0] * batch)
+    net.set_horizon(20.0, 0.01, True)
+    for _ in range(6):
+        net.advance(64)
+    for _ in range(8):
+        st = [net.state(b) for b in range(batch)]
+        assert len({round(s[1], 12) for s in st}) > 1
+        for b in range(batch):
+            net.set_state(b, st[b][0], st[b][1], st[b][2])
+        net.set_horizon(20.0, 0.01, False)
+        net.advance(64)
+        for b in range(batch):
+            r = net.order(b)
+            assert r.size > 0 and np.all(np.isfinite(r)) and np.all((r >= 0) & (r <= 1.0 + 1e-6))
+    net.close()

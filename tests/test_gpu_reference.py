@@ -107,7 +107,7 @@ def test_config1_dense_against_reference_programs(native, oracle_lib, ref, workd
     wg, _ = phase_dev(g, r64, 1.0)
     w32, _ = phase_dev(r32, r64, 1.0)
     assert np.median(wg) <= 2 * np.median(w32) + 1e-5, (float(np.median(wg)), float(np.median(w32)))
-    o64 = oracle_as_reload(oracle_lib, th, om, k=5, c=3.0, onthefly=True, seed=1, t1=100.0, dt=1.0)
+    o64 = oracle_as_reload(oracle_lib, th, om, k=5, c1=3.0, onthefly=True, seed=1, t1=100.0, dt=1.0)
     assert abs(float(np.mean(o64.order)) - mean(r64)) <= 1e-3
 
 
