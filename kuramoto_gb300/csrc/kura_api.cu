@@ -187,6 +187,9 @@ extern "C" void kura_destroy(kura_handle* h) {
 template <typename T> static cudaError_t dalloc(T** p, size_t count) {
   cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
   if (e == cudaSuccess) e = cudaMemset(*p, 0, std::max<size_t>(count, 1) * sizeof(T));
+  // the memset runs on the legacy default stream, which does not order with the non-blocking
+  // stream a handle may own: wait for it, so that no later copy on that stream lands first
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   return e;
 }
 

@@ -296,6 +296,8 @@ cudaError_t dalloc(kura_mlp* m, T** p, size_t count) {
   if (e == cudaSuccess) {
     m->allocs.push_back(*p);
     e = cudaMemset(*p, 0, sizeof(T) * std::max<size_t>(count, 1));
+    // the zero-fill runs on the legacy default stream, unordered with a non-blocking stream
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   }
   return e;
 }
@@ -387,6 +389,7 @@ int check_err(kura_mlp* m) {
   MLPCU(cudaMemcpy(&e, m->err, sizeof(int), cudaMemcpyDeviceToHost));
   if (e != 0) {
     cudaMemset(m->err, 0, sizeof(int));
+    cudaStreamSynchronize(0);
     return mlp_fail(KURA_ERR_BARRIER_TIMEOUT, "a tensor-core GEMM of the MLP timed out waiting for its operands");
   }
   return KURA_OK;

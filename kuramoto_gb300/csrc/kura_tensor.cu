@@ -537,6 +537,9 @@ const char* TensorEngine::last_error() { return g_terr.c_str(); }
 template <typename T> static cudaError_t zalloc(T** p, size_t count) {
   cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
   if (e == cudaSuccess) e = cudaMemset(*p, 0, std::max<size_t>(count, 1) * sizeof(T));
+  // the memset runs on the legacy default stream, which does not order with the non-blocking
+  // stream a handle may own: wait for it, so that no later copy on that stream lands first
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   return e;
 }
 
@@ -891,10 +894,12 @@ int TensorEngine::evaluate(int mode, int b, float* theta_out, float* coup_out) {
 
 int TensorEngine::sync_traj(std::vector<TrajG>& traj, bool to_device) {
   Impl& I = *d;
+  // on the engine's stream: the legacy-stream cudaMemcpy does not order with it
   if (to_device)
-    TCU(cudaMemcpy(I.traj, traj.data(), sizeof(TrajG) * I.B, cudaMemcpyHostToDevice));
+    TCU(cudaMemcpyAsync(I.traj, traj.data(), sizeof(TrajG) * I.B, cudaMemcpyHostToDevice, I.st));
   else
-    TCU(cudaMemcpy(traj.data(), I.traj, sizeof(TrajG) * I.B, cudaMemcpyDeviceToHost));
+    TCU(cudaMemcpyAsync(traj.data(), I.traj, sizeof(TrajG) * I.B, cudaMemcpyDeviceToHost, I.st));
+  TCU(cudaStreamSynchronize(I.st));
   return KURA_OK;
 }
 
