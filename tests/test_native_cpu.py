@@ -106,3 +106,13 @@ def test_oracle_cli_files(oracle_lib, tmp_path):
     assert sz("fs.dat") == (64 + 2 + 128) * 4
     first = open(base + ".out").readline()
     assert first.startswith("64 3 3.000000 1.000000 2.000000 1")
+
+
+def test_advance_and_horizon_validate_arguments_without_gpu(native):
+    """kura_advance and kura_set_horizon check their arguments before any device work."""
+    import ctypes
+    L = native.lib()
+    running = ctypes.c_int32(-1)
+    assert L.kura_advance(None, None, 10, ctypes.byref(running)) == -1
+    assert running.value == -1
+    assert L.kura_set_horizon(None, 1.0, 0.1, 1) == -1
