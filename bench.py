@@ -907,7 +907,7 @@ def main_windows(args, w):
         # per attempt: coefficients, 6 x (stage phases, GEMM), error, decision, 2 output kernels;
         # per step: the first-slope kernels (their GEMM is skipped once the slopes are on the device)
         line["gpu_launches"] = 17 * d["launches"] + 6 * steps
-        line["roofline"] = roofline_tensor(n, B, d, ms)
+        line["roofline"] = roofline_tensor(n, B, d, ms, args.workload)
     else:
         # one persistent launch per step; A is read once per RHS for the whole batch
         line["gpu_launches"] = d["launches"]
@@ -959,7 +959,15 @@ def roofline_hbm(bytes_per_launch, kernel_ms_per_launch, traffic=None):
             "kernel_ms_per_launch": round(kernel_ms_per_launch, 3)}
 
 
-def roofline_tensor(n, B, d, step_ms):
+def traffic_entry(workload, key):
+    try:
+        t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(workload)
+        return t.get(key) if t else None
+    except Exception:
+        return None
+
+
+def roofline_tensor(n, B, d, step_ms, workload=None):
     """The coupling GEMM: one launch is every trajectory's RHS, C = (N A) [cos|sin]: 4 N^2 B
     algorithmic flops (2 columns x 2 flops per multiply-add), 8 N^2 B issued (hi and lo columns).
     Its duration is the CUDA-event time of the GEMM launches the engine sampled in the timed
@@ -976,7 +984,7 @@ def roofline_tensor(n, B, d, step_ms):
     hbm = peaks.get("hbm_gbs", 6800.0)
     a_gbs = 2.0 * n * n / (per / 1e3) / 1e9 if per > 0 else 0.0
     out = {"bound": "tensor", "achieved": round(ach, 1), "peak": peak, "unit": "TFLOP/s",
-           "frac": round(ach / peak, 4), "traffic": None, "peak_source": src,
+           "frac": round(ach / peak, 4), "traffic": traffic_entry(workload, "bytes_per_launch"), "peak_source": src,
            "flops_per_launch": flops, "issued_flops_per_launch": 2 * flops,
            "kernel_ms_per_launch": round(per, 4), "launches_sampled": d["coupling_launches"],
            "whole_step_tflops": round(step_tf, 1), "whole_step_frac": round(step_tf / peak, 4),
