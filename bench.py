@@ -502,7 +502,12 @@ def main_multi(args, w):
                         "frac": round(achieved / hbm, 4), "traffic": traffic,
                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                         "bytes_per_unit": STATE_BYTES,
-                        "kernel_ms_per_launch": round(res["kernel_ms"] / args.steps, 3)}
+                        "kernel_ms_per_launch": round(res["kernel_ms"] / args.steps, 3),
+                        "binding": {"kind": "latency: the networks' state stays in L2; the integration ends when "
+                                            "its longest networks (the most accepted steps) end",
+                                    "accepted_steps_max_network": int(res["acc"].max()),
+                                    "us_per_step_of_longest_network": round(res["kernel_ms"] / args.steps * 1e3 /
+                                                                            max(int(res["acc"].max()), 1), 3)}}
     line["clocks"] = res["clocks"]
     line["launch_shape"] = {"cluster_size": res["shape"][0], "block_threads": res["shape"][1],
                             "grid": res["shape"][2], "heavy_networks_in_large_clusters": res["shape"][3],
