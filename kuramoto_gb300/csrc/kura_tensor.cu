@@ -376,18 +376,28 @@ __global__ void k_t_out_partial(TView v, const TrajG* traj, const float* t_eval,
   const size_t bl = initial ? ((size_t)T.rot_y * v.bp + b) * v.np : ((size_t)(T.rot_y ^ 1) * v.bp + b) * v.np;
   // after the accept, k1 of the step sits in the k7 slot and vice versa
   const int k1s = slot_k7(T.rot_g), k7s = slot_k1(T.rot_g);
+  __shared__ float sw[9];  // the record's weights: W[0..6], then the time offset hi and lo
   for (int c = 0; c < nrec; ++c) {
-    float W[7] = {0, 0, 0, 0, 0, 0, 0};
-    float mh = 0.f, ml = 0.f;
-    if (!initial) {
-      const double hs = T.t - T.t_last, dl = (double)t_eval[T.eval_i + c] - T.t_last, x = dl / hs;
-      for (int j = 0; j < 7; ++j) {
-        const double cc = ((P_TAB[j][3] * x + P_TAB[j][2]) * x + P_TAB[j][1]) * x * x + P_TAB[j][0] * x;
-        W[j] = (float)(hs * cc);
+    // the weights in double, once per block (FP64 is a small fraction of this GPU's FP32 rate:
+    // computed by every thread they cost more than the record's memory traffic)
+    if (threadIdx.x == 0) {
+      for (int j = 0; j < 9; ++j) sw[j] = 0.f;
+      if (!initial) {
+        const double hs = T.t - T.t_last, dl = (double)t_eval[T.eval_i + c] - T.t_last, x = dl / hs;
+        for (int j = 0; j < 7; ++j) {
+          const double cc = ((P_TAB[j][3] * x + P_TAB[j][2]) * x + P_TAB[j][1]) * x * x + P_TAB[j][0] * x;
+          sw[j] = (float)(hs * cc);
+        }
+        const float mh0 = (float)dl;
+        sw[7] = mh0;
+        sw[8] = (float)(dl - (double)mh0);
       }
-      mh = (float)dl;
-      ml = (float)(dl - (double)mh);
     }
+    __syncthreads();
+    float W[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) W[j] = sw[j];
+    const float mh = sw[7], ml = sw[8];
     float ax = 0.f, ay = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n; i += gridDim.x * blockDim.x) {
       float gsum = 0.f;
