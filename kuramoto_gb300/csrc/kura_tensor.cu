@@ -32,6 +32,11 @@ namespace kura {
 namespace {
 
 constexpr int T_MAXC = 32;  // output crossings handled per step
+// K per pipeline stage of the coupling GEMM (32: 64-byte swizzle rows; 64: 128-byte rows)
+#ifndef KURA_GEMM_BK
+#define KURA_GEMM_BK 32
+#endif
+constexpr int TE_BK = KURA_GEMM_BK;
 constexpr int T_RBLK = 256; // rows per block of the reduction kernels
 
 struct TCoef {
@@ -607,8 +612,9 @@ int TensorEngine::init(int64_t n, int k, int batch, int seed, double atol, doubl
     for (cudaEvent_t& e : I.gev) TCU(cudaEventCreate(&e));
   // X is [4 bp][np]: a work unit's column block is 4 * x_bph(bp) rows (its hi + lo columns),
   // of which the A_lo pass reads the first half
-  if (make_tmap_bf16(&I.tmA, I.Ahi, np, np, TG_BM) || make_tmap_bf16(&I.tmX, I.X, np, 4 * bp, 4 * x_bph(I.bp)) ||
-      make_tmap_bf16(&I.tmXhi, I.X, np, 4 * bp, 2 * x_bph(I.bp))) {
+  if (make_tmap_bf16(&I.tmA, I.Ahi, np, np, TG_BM, TE_BK) ||
+      make_tmap_bf16(&I.tmX, I.X, np, 4 * bp, 4 * x_bph(I.bp), TE_BK) ||
+      make_tmap_bf16(&I.tmXhi, I.X, np, 4 * bp, 2 * x_bph(I.bp), TE_BK)) {
     g_terr = "cuTensorMapEncodeTiled failed";
     return KURA_ERR_CUDA;
   }
@@ -644,7 +650,7 @@ int TensorEngine::generate_adjacency() {
   TCU(cudaGetLastError());
   TCU(cudaStreamSynchronize(I.st));
   if (bits) cudaFree(bits);
-  if (need_lo && make_tmap_bf16(&I.tmAlo, I.Alo, I.np, I.np, TG_BM)) {
+  if (need_lo && make_tmap_bf16(&I.tmAlo, I.Alo, I.np, I.np, TG_BM, TE_BK)) {
     g_terr = "cuTensorMapEncodeTiled failed";
     return KURA_ERR_CUDA;
   }
@@ -665,7 +671,7 @@ int TensorEngine::set_adjacency(const float* adj_host) {
   TCU(cudaGetLastError());
   TCU(cudaStreamSynchronize(I.st));
   cudaFree(dadj);
-  if (make_tmap_bf16(&I.tmAlo, I.Alo, I.np, I.np, TG_BM)) {
+  if (make_tmap_bf16(&I.tmAlo, I.Alo, I.np, I.np, TG_BM, TE_BK)) {
     g_terr = "cuTensorMapEncodeTiled failed";
     return KURA_ERR_CUDA;
   }
@@ -726,7 +732,7 @@ static cudaError_t launch_gemm(TensorEngine::Impl& I, const TCoef* src, int mode
   constexpr int BP = NCOL / 4;  // trajectories per work unit
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, I.device);
-  const int mtiles = I.np / (2 * TG_BM), ktiles = I.np / TG_BK;  // groups of two row tiles
+  const int mtiles = I.np / (2 * TG_BM), ktiles = I.np / TE_BK;  // groups of two row tiles
   const int nsplit = I.bp / BP, xstride = 4 * BP;
   const int grid = std::min(mtiles * nsplit, sms);
   // Units of two row tiles fill whole waves of the grid; the rest run as one-tile units, when
@@ -742,18 +748,18 @@ static cudaError_t launch_gemm(TensorEngine::Impl& I, const TCoef* src, int mode
   }
   const unsigned long long limit = 20000000000ull;
   if (I.has_lo) {
-    auto kl = k_tensor_gemm<NCOL / 2, LoEpi<BP>, 2>;
-    cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL / 2, 2>::SMEM);
+    auto kl = k_tensor_gemm<NCOL / 2, LoEpi<BP>, 2, TE_BK>;
+    cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL / 2, 2, TE_BK>::SMEM);
     LoEpi<BP> le{v, src};
-    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2, 2>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, big, ktiles, nsplit, xstride, le,
+    kl<<<grid, TG_THREADS, TGCfg<NCOL / 2, 2, TE_BK>::SMEM, I.st>>>(I.tmAlo, I.tmXhi, mtiles, big, ktiles, nsplit, xstride, le,
                                                              I.err, limit, run_flag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  auto k = k_tensor_gemm<NCOL, KuraEpi<BP>, 2>;
-  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL, 2>::SMEM);
+  auto k = k_tensor_gemm<NCOL, KuraEpi<BP>, 2, TE_BK>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TGCfg<NCOL, 2, TE_BK>::SMEM);
   KuraEpi<BP> ep{v, src, 1.0f / (float)I.n, I.has_lo ? 1 : 0};
-  k<<<grid, TG_THREADS, TGCfg<NCOL, 2>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, big, ktiles, nsplit, xstride, ep, I.err, limit,
+  k<<<grid, TG_THREADS, TGCfg<NCOL, 2, TE_BK>::SMEM, I.st>>>(I.tmA, I.tmX, mtiles, big, ktiles, nsplit, xstride, ep, I.err, limit,
                                                    run_flag);
   return cudaGetLastError();
 }

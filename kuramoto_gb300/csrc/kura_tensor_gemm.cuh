@@ -22,13 +22,15 @@ constexpr int TG_ROWB = TG_BK * 2;  // bytes per tile row
 constexpr int TG_THREADS = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 
 // NCOL columns per work unit, MT row tiles of 128 per work unit (sharing every X stage: MT = 2
-// halves the operand bytes per flop that X costs)
-template <int NCOL, int MT = 1> struct TGCfg {
+// halves the operand bytes per flop that X costs), BK of K per stage: 32 (rows of 64 bytes, the
+// 64-byte swizzle) or 64 (rows of 128 bytes, the 128-byte swizzle)
+template <int NCOL, int MT = 1, int BK = TG_BK> struct TGCfg {
   static constexpr int NMMA = NCOL > 256 ? 256 : NCOL;  // N of one MMA instruction
   static constexpr int NH = NCOL / NMMA;                // MMAs per K step and row tile
-  static constexpr int A1_BYTES = TG_BM * TG_BK * 2;    // one row tile of a stage
+  static constexpr int ROWB = BK * 2;                  // bytes per operand row of a stage
+  static constexpr int A1_BYTES = TG_BM * BK * 2;       // one row tile of a stage
   static constexpr int A_BYTES = MT * A1_BYTES;
-  static constexpr int X_BYTES = NCOL * TG_BK * 2;
+  static constexpr int X_BYTES = NCOL * BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + X_BYTES;
   // as many stages as 225 KB of the 227 KB per CTA hold (at most 8): the bytes in flight hide
   // the latency of the operand loads
@@ -39,6 +41,7 @@ template <int NCOL, int MT = 1> struct TGCfg {
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /* align */ + 256 /* barriers */;
   static_assert(NCOL % 16 == 0 && NCOL <= 512 && MT * NCOL <= 512, "NCOL");
   static_assert(STAGES >= 2, "stages");
+  static_assert(BK == 32 || BK == 64, "BK");
 };
 
 // Work units: (MT row tiles of 128, column block); column block sp covers X rows
@@ -50,12 +53,12 @@ template <int NCOL, int MT = 1> struct TGCfg {
 // every thread of warps 1-4 with taddr = TMEM address of this thread's accumulator row
 // (lane field set, column 0).  With NCOL <= 256 the accumulator is double-buffered in TMEM,
 // so one unit's epilogue overlaps the next unit's MMAs.
-template <int NCOL, class Epi, int MT = 1>
+template <int NCOL, class Epi, int MT = 1, int BK = TG_BK>
 __global__ void __launch_bounds__(TG_THREADS, 1)
     k_tensor_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmX, int mtiles,
                   int big_tiles, int ktiles, int nsplit, int xstride, Epi epi, int* err, unsigned long long limit_ns,
                   const int* run_flag) {
-  using C = TGCfg<NCOL, MT>;
+  using C = TGCfg<NCOL, MT, BK>;
   if (run_flag && *run_flag == 0) return;  // nothing to compute (every column inactive)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -123,10 +126,10 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
           umma::mbar_arrive_expect_tx(&full[s], mtu * C::A1_BYTES + C::X_BYTES);
 #pragma unroll
           for (int mt = 0; mt < MT; ++mt)
-            if (mt < mtu) umma::tma_load_2d(st + mt * C::A1_BYTES, &tmA, &full[s], kt * TG_BK, (rt0 + mt) * TG_BM);
+            if (mt < mtu) umma::tma_load_2d(st + mt * C::A1_BYTES, &tmA, &full[s], kt * BK, (rt0 + mt) * TG_BM);
 #pragma unroll
           for (int h = 0; h < (NCOL + 255) / 256; ++h)
-            umma::tma_load_2d(st + C::A_BYTES + h * 256 * TG_ROWB, &tmX, &full[s], kt * TG_BK, xr0 + h * 256);
+            umma::tma_load_2d(st + C::A_BYTES + h * 256 * C::ROWB, &tmX, &full[s], kt * BK, xr0 + h * 256);
           ++issued;
           if (++s == C::STAGES) { s = 0; ph ^= 1; }
         }
@@ -167,14 +170,16 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
           const uint32_t a0 = umma::smem_u32(smem + s * C::STAGE_BYTES);
           const uint32_t x0 = a0 + C::A_BYTES;
 #pragma unroll
-          for (int kk = 0; kk < TG_BK / 16; ++kk) {
+          for (int kk = 0; kk < BK / 16; ++kk) {
 #pragma unroll
             for (int mt = 0; mt < MT; ++mt) {
               if (mt >= mtu) break;
-              const uint64_t ad = umma::sw64_desc(a0 + mt * C::A1_BYTES + kk * 32);
+              const uint32_t aa = a0 + mt * C::A1_BYTES + kk * 32;
+              const uint64_t ad = BK == 64 ? umma::sw128_desc(aa) : umma::sw64_desc(aa);
 #pragma unroll
               for (int h = 0; h < C::NH; ++h) {
-                const uint64_t xd = umma::sw64_desc(x0 + h * C::NMMA * TG_ROWB + kk * 32);
+                const uint32_t xa = x0 + h * C::NMMA * C::ROWB + kk * 32;
+                const uint64_t xd = BK == 64 ? umma::sw128_desc(xa) : umma::sw64_desc(xa);
                 umma::mma_bf16(tacc + mt * NCOL + h * C::NMMA, ad, xd, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
               }
             }
@@ -223,7 +228,8 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
 typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-inline int make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t k, uint64_t rows, uint32_t box_rows) {
+inline int make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t k, uint64_t rows, uint32_t box_rows,
+                          int bk = TG_BK) {
   static PFN_encodeTiled fn = nullptr;
   if (!fn) {
     void* f = nullptr;
@@ -235,10 +241,11 @@ inline int make_tmap_bf16(CUtensorMap* map, const void* base, uint64_t k, uint64
   }
   cuuint64_t dims[2] = {k, rows};
   cuuint64_t strides[1] = {k * 2};
-  cuuint32_t box[2] = {(cuuint32_t)TG_BK, box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)bk, box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : -2;
 }
