@@ -40,6 +40,9 @@ WORKLOADS = {
     # the reference's default dense case (configs: N=5000, K=5, c=3, Cauchy, theta0=0, t=100, dt=1)
     "dense5000": dict(n=5000, k=5, coupling=0, cs=[3.0], normal=False, init=0.0, t1=100.0, dt=1.0, atol=1e-6,
                       rtol=0.0, shared_theta=True, fresh=True),
+    # the same with N*A stored as int8 (exact for the volcano rule): 25 MB, a quarter of the bytes per RHS
+    "dense5000i8": dict(n=5000, k=5, coupling=0, cs=[3.0], normal=False, init=0.0, t1=100.0, dt=1.0, atol=1e-6,
+                        rtol=0.0, shared_theta=True, fresh=True, adj_storage=1),
     # the plain FP32 path at N=65536 (17.2 GB adjacency read once per RHS; x8: shared by 8
     # trajectories of one pass), Cauchy omega, theta0 uniform in [0, 2pi); the Cauchy
     # outliers of N=65536 force steps of ~1e-4, so the horizon is short

@@ -66,6 +66,31 @@ __device__ __forceinline__ uint4 ld_stream_u4(const int8_t* p) {
 __device__ __forceinline__ float i8_to_f(uint32_t w_biased, int j) {
   return __int_as_float((int)__byte_perm(w_biased, 0x4B000000u, 0x7540u + (unsigned)j)) - 8388736.0f;
 }
+// Packed FP32 pairs (sm_100 and later): one instruction, each half rounded as the scalar
+// operation.  (a.lo*b.lo + c.lo, a.hi*b.hi + c.hi):
+__device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ float2 unpack_f2(unsigned long long v) {
+  float2 r;
+  asm("mov.b64 {%0,%1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+// byte j of w0 and of w1 (biased by 0x80, as for i8_to_f) as the exact float pair
+// (lo: w0, hi: w1): both placed under the exponent of 2^23, then 2^23 + 128 subtracted from
+// the pair in one packed add
+__device__ __forceinline__ unsigned long long i8_pair_to_f2(uint32_t w0, uint32_t w1, int j) {
+  const uint32_t lo = __byte_perm(w0, 0x4B000000u, 0x7540u + (unsigned)j);
+  const uint32_t hi = __byte_perm(w1, 0x4B000000u, 0x7540u + (unsigned)j);
+  const unsigned long long bias = 0xCB000080CB000080ull;  // (-8388736.0f, -8388736.0f)
+  unsigned long long d;
+  asm("{\n\t.reg .b64 t;\n\tmov.b64 t, {%1,%2};\n\tadd.rn.f32x2 %0, t, %3;\n\t}"
+      : "=l"(d) : "r"(lo), "r"(hi), "l"(bias));
+  return d;
+}
 // 16 bytes global -> shared without a register round trip (L2 only); src_bytes 0 zero-fills
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, int src_bytes) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
@@ -121,9 +146,11 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
   off[4] = o; o += align16(sl * 4);                      // slice
   off[5] = o; o += align16(16 * 4);                      // flags
   off[6] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? rows * 4 : 0);   // factor bits
-  // x tile; the int8 product's has 2 (cos, sin) pairs of padding per 16 columns
+  // x tile; the int8 product's holds (cos, cos, sin, sin) per column and one such float4 of
+  // padding per 16 columns for one trajectory, (cos, sin) and two pairs of padding for a batch
   off[7] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? 0
-                           : coup == COUP_DENSE_I8 ? bmax * ((bmax == 1 ? CT_I8 : CT) / 16) * I8_CHUNK * 8
+                           : coup == COUP_DENSE_I8 ? (bmax == 1 ? (CT_I8 / 16) * I8_CHUNK4 * 16
+                                                                : bmax * (CT / 16) * I8_CHUNK * 8)
                                                    : bmax * ((bmax == 1 ? CT_F1 : CT) / 4) * F_CHUNK * 8);
   // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
   off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
@@ -763,20 +790,70 @@ struct Engine {
   }
 
   // A (rows r0..r1 of this CTA) times the (cos, sin) of every trajectory.  x is
-  // staged in shared memory one column tile at a time; each warp works on RG rows, each
-  // lane on 16-byte chunks of them, A_STAGES chunks per row in flight.
+  // staged in shared memory one column tile at a time; each warp works on up to RG rows,
+  // each lane on 16-byte chunks of them.
   static constexpr int CTF = BMAX == 1 ? CT_F1 : CT;  // columns per x tile of the float product
   // A lane's 4 columns of x are 32 bytes from the next lane's, so back to back they would
   // fall on four of the eight 16-byte bank groups; a stride of F_CHUNK = 6 (cos, sin) pairs
   // (48 bytes) per 4 columns uses all eight.
   static constexpr int CTFP = CTF / 4 * F_CHUNK;
+  // One x tile for the NR rows this warp holds.  A streams through the warp's ring of
+  // A_STAGES * RG chunk slots with cp.async: every lane copies its own 16 bytes of each
+  // row, ST = A_STAGES * RG / NR column steps ahead, and reads back only what it copied,
+  // so the ring needs no barrier and holds no registers per byte in flight.  A warp with
+  // fewer rows (small N, the last pass) keeps as many bytes in flight with more steps.
+  // The prologue's copies start before the x tile has landed; neither part holds a barrier,
+  // so warps with different NR run side by side between the caller's barriers.
+  template <int NR>
+  __device__ __forceinline__ void mv_f32_prologue(float4* my, const float* const (&src)[RG], int c0, int nit) {
+    constexpr int ST = A_STAGES * RG / NR;
+    static_assert(ST * NR <= A_STAGES * RG, "ring slots");
+#pragma unroll
+    for (int s = 0; s < ST - 1; ++s) {
+      if (s < nit)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) cp_async16(my + (s * NR + q) * 32, src[q] + c0 + 128 * s, 16);
+      cp_async_commit();
+    }
+    cp_async_wait<ST - 1>();  // this thread's copies of the x tile, committed before, have landed
+  }
+  template <int NR>
+  __device__ __forceinline__ void mv_f32_steps(float4* my, const float* const (&src)[RG], int c0, int nit,
+                                               float (&acc)[RG][BMAX][2]) {
+    constexpr int ST = A_STAGES * RG / NR;
+    for (int it = 0; it < nit; ++it) {
+      const int ahead = it + ST - 1;
+      if (ahead < nit) {
+        const int sl = ahead % ST;
+#pragma unroll
+        for (int q = 0; q < NR; ++q) cp_async16(my + (sl * NR + q) * 32, src[q] + c0 + 128 * ahead, 16);
+      }
+      cp_async_commit();
+      cp_async_wait<ST - 1>();  // the chunks of step it have landed
+      const int sl = it % ST;
+      float4 a[NR];
+#pragma unroll
+      for (int q = 0; q < NR; ++q) a[q] = my[(sl * NR + q) * 32];
+      const int cc = lane * 4 + 128 * it;
+#pragma unroll
+      for (int b = 0; b < BMAX; ++b) {
+        if (b < B) {
+          const float4* xp = reinterpret_cast<const float4*>(xt + b * CTFP + (cc >> 2) * F_CHUNK);
+          float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
+#pragma unroll
+          for (int q = 0; q < NR; ++q) {
+            acc[q][b][0] += a[q].x * x01.x + a[q].y * x01.z + a[q].z * x23.x + a[q].w * x23.z;
+            acc[q][b][1] += a[q].x * x01.y + a[q].y * x01.w + a[q].z * x23.y + a[q].w * x23.w;
+          }
+        }
+      }
+    }
+    cp_async_wait<0>();
+  }
+
   __device__ void dense_matvec() {
     const int ld = p.ld;
     const int rows_per_pass = KW * RG;
-    // A streams through a per-warp ring in shared memory with cp.async: every lane copies its
-    // own 16 bytes of each of the warp's RG rows, A_STAGES column steps ahead, and reads back
-    // only what it copied, so the ring needs no barrier and holds no registers per byte in
-    // flight.  Rows past the CTA's block are zero-filled.
     float4* my = ring + (size_t)warp * (A_STAGES * RG * 32) + lane;
     for (int pr0 = r0; pr0 < r1; pr0 += rows_per_pass) {
       float acc[RG][BMAX][2];
@@ -784,78 +861,59 @@ struct Engine {
       for (int q = 0; q < RG; ++q)
 #pragma unroll
         for (int b = 0; b < BMAX; ++b) acc[q][b][0] = acc[q][b][1] = 0.f;
-      // warp w takes rows pr0 + w + KW*q of the pass, so small row blocks keep every warp busy
+      // warp w takes rows pr0 + w + KW*q of the pass, so small row blocks keep every warp
+      // busy; its nr rows in the CTA's block are q < nr
       const int row0 = pr0 + warp;
+      const int nr = r1 > row0 ? min(RG, (r1 - row0 + KW - 1) / KW) : 0;
       const float* src[RG];
-      int nb[RG];
 #pragma unroll
       for (int q = 0; q < RG; ++q) {
         const int row = row0 + KW * q;
-        nb[q] = row < r1 ? 16 : 0;
         src[q] = p.adj + (size_t)(row < r1 ? row : r0) * ld + lane * 4;
       }
-      for (int c0 = 0; c0 < ld; c0 += CTF) {
-        __syncthreads();
-        const int cw = min(CTF, ld - c0);
-        for (int t = tid; t < B * CTF; t += KT) {
-          int b = t / CTF, c = t - b * CTF;
-          xt[b * CTFP + (c >> 2) * F_CHUNK + (c & 3)] =
-              (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
-        }
-        __syncthreads();
-        // column steps of this lane: cc = lane*4 + 128*it < cw (cw is a multiple of 32)
+      int c0 = 0;
+      for (; c0 < ld; c0 += CTF) {
+        __syncthreads();  // the previous tile's readers are done
+        const int cw = min(CTF, ld - c0);  // a multiple of 32
+        // the x tile, 16 bytes (two columns) per copy, in one commit group ahead of the ring's
+        for (int b = 0; b < B; ++b)
+          for (int c = 2 * tid; c < cw; c += 2 * KT)
+            cp_async16(xt + b * CTFP + (c >> 2) * F_CHUNK + (c & 3), p.xbuf + ((size_t)xpar * B + b) * ld + c0 + c,
+                       16);
+        cp_async_commit();
+        // column steps of this lane: cc = lane*4 + 128*it < cw
         const int nit = (cw - lane * 4 + 127) >> 7;
-#pragma unroll
-        for (int s = 0; s < A_STAGES - 1; ++s) {
-          if (s < nit)
-#pragma unroll
-            for (int q = 0; q < RG; ++q) cp_async16(my + (s * RG + q) * 32, src[q] + c0 + 128 * s, nb[q]);
-          cp_async_commit();
-        }
-        for (int it = 0; it < nit; ++it) {
-          const int ahead = it + A_STAGES - 1;
-          if (ahead < nit) {
-            const int sl = ahead % A_STAGES;
-#pragma unroll
-            for (int q = 0; q < RG; ++q) cp_async16(my + (sl * RG + q) * 32, src[q] + c0 + 128 * ahead, nb[q]);
-          }
-          cp_async_commit();
-          cp_async_wait<A_STAGES - 1>();  // the chunks of step it have landed
-          const int sl = it % A_STAGES;
-          float4 a[RG];
-#pragma unroll
-          for (int q = 0; q < RG; ++q) a[q] = my[(sl * RG + q) * 32];
-          const int cc = lane * 4 + 128 * it;
-#pragma unroll
-          for (int b = 0; b < BMAX; ++b) {
-            if (b < B) {
-              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTFP + (cc >> 2) * F_CHUNK);
-              float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
-#pragma unroll
-              for (int q = 0; q < RG; ++q) {
-                acc[q][b][0] += a[q].x * x01.x + a[q].y * x01.z + a[q].z * x23.x + a[q].w * x23.z;
-                acc[q][b][1] += a[q].x * x01.y + a[q].y * x01.w + a[q].z * x23.y + a[q].w * x23.w;
-              }
-            }
-          }
-        }
-        cp_async_wait<0>();
+        if (nr == 4) mv_f32_prologue<4>(my, src, c0, nit);
+        else if (nr == 3) mv_f32_prologue<3>(my, src, c0, nit);
+        else if (nr == 2) mv_f32_prologue<2>(my, src, c0, nit);
+        else if (nr == 1) mv_f32_prologue<1>(my, src, c0, nit);
+        else cp_async_wait<0>();
+        __syncthreads();  // every thread's part of the x tile has landed
+        if (nr == 4) mv_f32_steps<4>(my, src, c0, nit, acc);
+        else if (nr == 3) mv_f32_steps<3>(my, src, c0, nit, acc);
+        else if (nr == 2) mv_f32_steps<2>(my, src, c0, nit, acc);
+        else if (nr == 1) mv_f32_steps<1>(my, src, c0, nit, acc);
       }
+      const int xt_c0 = c0 - CTF;  // first column of the tile still staged
 #pragma unroll
       for (int q = 0; q < RG; ++q)
+        if (q < nr)
 #pragma unroll
-        for (int b = 0; b < BMAX; ++b) {
-          acc[q][b][0] = warp_sum(acc[q][b][0]);
-          acc[q][b][1] = warp_sum(acc[q][b][1]);
-        }
-      // lane q*BMAX+b finishes row row0+q of trajectory b
+          for (int b = 0; b < BMAX; ++b) {
+            acc[q][b][0] = warp_sum(acc[q][b][0]);
+            acc[q][b][1] = warp_sum(acc[q][b][1]);
+          }
+      // lane q*BMAX+b finishes row row0+q of trajectory b; its own (cos, sin) come from the
+      // staged tile when the last tile holds the row
 #pragma unroll
       for (int q = 0; q < RG; ++q)
 #pragma unroll
         for (int b = 0; b < BMAX; ++b) {
           int row = row0 + KW * q;
           if (lane == q * BMAX + b && b < B && row < r1 && sb[b].active) {
-            float2 x = __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + row]);
+            const int c = row - xt_c0;
+            const float2 x = c >= 0 ? xt[b * CTFP + (c >> 2) * F_CHUNK + (c & 3)]
+                                    : __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + row]);
             epilogue(b, row, acc[q][b][0], acc[q][b][1], x.x, x.y);
           }
         }
@@ -863,13 +921,110 @@ struct Engine {
   }
 
   static constexpr int CTX = BMAX == 1 ? CT_I8 : CT;  // columns per x tile of the int8 product
-  // Each lane's 16 columns of x are 128 bytes apart from the next lane's.  Stored back to
-  // back, all 32 lanes would read the same four banks; a stride of I8_CHUNK = 18 (cos, sin)
-  // pairs (144 bytes) per 16 columns spreads them over eight 16-byte bank groups.
-  static constexpr int CTXP = CTX / 16 * I8_CHUNK;
-  // one pass over RG rows per warp (rows pr0 + warp + KW*q), CPL int8 columns per lane and load
-  template <int RG, int CPL>
+  // The int8 product's x tile holds per column the float4 (cos, cos, sin, sin), so that one
+  // packed FP32 FMA multiplies the converted bytes of two rows by the same column.  A lane's
+  // 16 columns start I8_CHUNK4 = 17 float4 (272 bytes) after the previous lane's, which puts
+  // the 8 lanes of each phase of a 16-byte shared-memory read on distinct banks.
+  static constexpr int CTXP = CTX / 16 * I8_CHUNK4;  // float4 per trajectory
+  // The columns [c0, c0 + cw) of the staged tile for the first RGT of the pass's RG_I8 rows of
+  // this warp (rows pr0 + warp + KW*q), CPL int8 columns per lane and load; rows 2qp and 2qp+1
+  // share the packed accumulators acc[qp].  No barrier inside: warps with different RGT run
+  // side by side between the tile barriers of the caller.
+  static constexpr int RG_I8 = 8;
+  template <int RGT, int CPL>
+  __device__ __forceinline__ void mv_i8_tile(unsigned long long (&acc)[RG_I8 / 2][2], int row0, int c0, int cw) {
+    static_assert(RGT % 2 == 0 && RGT <= RG_I8, "rows are taken in pairs");
+    constexpr int NWD = CPL / 4;
+    const int ld8 = p.ld8;
+    const float4* xt4 = reinterpret_cast<const float4*>(xt);
+    for (int cc = lane * CPL; cc < cw; cc += 32 * CPL) {
+      uint32_t a[RGT][NWD];
+#pragma unroll
+      for (int q = 0; q < RGT; ++q) {
+        const int row = row0 + KW * q;
+        const int8_t* src = p.adj8 + (size_t)row * ld8 + c0 + cc;
+        const uint4 v = (row < r1) ? ld_stream_u4(src) : make_uint4(0u, 0u, 0u, 0u);
+        a[q][0] = v.x;
+        a[q][1 % NWD] = v.y;
+        a[q][2 % NWD] = v.z;
+        a[q][3 % NWD] = v.w;
+#pragma unroll
+        for (int wd = 0; wd < NWD; ++wd) a[q][wd] ^= 0x80808080u;
+      }
+#pragma unroll
+      for (int wd = 0; wd < NWD; ++wd) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          // ((cos, cos), (sin, sin)) of column cc + 4*wd + j
+          const ulonglong2 xj = *reinterpret_cast<const ulonglong2*>(xt4 + (cc >> 4) * I8_CHUNK4 + 4 * wd + j);
+#pragma unroll
+          for (int qp = 0; qp < RGT / 2; ++qp) {
+            const unsigned long long kp = i8_pair_to_f2(a[2 * qp][wd], a[2 * qp + 1][wd], j);
+            acc[qp][0] = ffma2(kp, xj.x, acc[qp][0]);
+            acc[qp][1] = ffma2(kp, xj.y, acc[qp][1]);
+          }
+        }
+      }
+    }
+  }
+  // one pass over the RG_I8 rows per warp of one trajectory
   __device__ void mv_i8_pass(int pr0) {
+    constexpr int CPL = 16;
+    const int ld = p.ld, ld8 = p.ld8;
+    float4* xt4 = reinterpret_cast<float4*>(xt);
+    // [qp][0]: (sum k cos) of rows (2qp, 2qp+1); [qp][1]: the same for sin
+    unsigned long long acc[RG_I8 / 2][2];
+#pragma unroll
+    for (int q = 0; q < RG_I8 / 2; ++q) acc[q][0] = acc[q][1] = 0ull;
+    const int row0 = pr0 + warp;
+    const int nr = r1 > row0 ? min(RG_I8, (r1 - row0 + KW - 1) / KW) : 0;
+    int c0 = 0;
+    for (; c0 < ld8; c0 += CTX) {
+      __syncthreads();
+      const int cw = min(CTX, ld8 - c0);  // a multiple of 16
+      for (int c = tid; c < cw; c += KT) {
+        const float2 x = __ldcg(&p.xbuf[(size_t)xpar * ld + c0 + c]);
+        xt4[(c >> 4) * I8_CHUNK4 + (c & 15)] = make_float4(x.x, x.x, x.y, x.y);
+      }
+      __syncthreads();
+      // a warp with at most 4 rows in the pass (small N, the last pass) converts no bytes of
+      // the absent ones
+      if (nr <= 4) mv_i8_tile<4, CPL>(acc, row0, c0, cw);
+      else mv_i8_tile<RG_I8, CPL>(acc, row0, c0, cw);
+    }
+    float accf[RG_I8][2];
+#pragma unroll
+    for (int qp = 0; qp < RG_I8 / 2; ++qp)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const float2 u = unpack_f2(acc[qp][v]);
+        accf[2 * qp][v] = warp_sum(u.x);
+        accf[2 * qp + 1][v] = warp_sum(u.y);
+      }
+    // the row's own (cos, sin) from the staged tile when the last tile holds it
+    const int xt_c0 = c0 - CTX;
+#pragma unroll
+    for (int q = 0; q < RG_I8; ++q) {
+      const int row = row0 + KW * q;
+      if (lane == q && row < r1 && sb[0].active) {
+        const int c = row - xt_c0;
+        float2 x;
+        if (c >= 0) {
+          const float4 v = xt4[(c >> 4) * I8_CHUNK4 + (c & 15)];
+          x = make_float2(v.x, v.z);
+        } else {
+          x = __ldcg(&p.xbuf[(size_t)xpar * ld + row]);
+        }
+        epilogue(0, row, accf[q][0] * p.invn, accf[q][1] * p.invn, x.x, x.y);
+      }
+    }
+  }
+  // The batch form: x tile of (cos, sin) pairs, I8_CHUNK = 18 pairs (144 bytes) per 16
+  // columns, and one scalar FMA per byte, trajectory and sum; the register budget of eight
+  // trajectories leaves no room for the packed form's operands.
+  static constexpr int CTXB = CTX / 16 * I8_CHUNK;  // float2 per trajectory
+  template <int RG, int CPL>
+  __device__ void mv_i8_pass_batch(int pr0) {
     constexpr int NWD = CPL / 4;
     const int ld = p.ld, ld8 = p.ld8;
     float acc[RG][BMAX][2];
@@ -883,7 +1038,7 @@ struct Engine {
       const int cw = min(CTX, ld8 - c0);  // a multiple of 16
       for (int t = tid; t < B * CTX; t += KT) {
         int b = t / CTX, c = t - b * CTX;
-        xt[b * CTXP + (c >> 4) * I8_CHUNK + (c & 15)] =
+        xt[b * CTXB + (c >> 4) * I8_CHUNK + (c & 15)] =
             (c < cw) ? __ldcg(&p.xbuf[((size_t)xpar * B + b) * ld + c0 + c]) : make_float2(0.f, 0.f);
       }
       __syncthreads();
@@ -912,7 +1067,7 @@ struct Engine {
 #pragma unroll
           for (int b = 0; b < BMAX; ++b) {
             if (b < B) {
-              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTXP + (cc >> 4) * I8_CHUNK + 4 * wd);
+              const float4* xp = reinterpret_cast<const float4*>(xt + b * CTXB + (cc >> 4) * I8_CHUNK + 4 * wd);
               const float4 x01 = xp[0], x23 = xp[1];  // (c0,s0,c1,s1), (c2,s2,c3,s3)
 #pragma unroll
               for (int q = 0; q < RG; ++q) {
@@ -947,11 +1102,17 @@ struct Engine {
   // The same product with A stored as the integers N*A (int8, exact for the reference's
   // volcano rule, K <= 127): a quarter of the HBM bytes.  Each lane streams 16 columns of
   // 8 rows (one trajectory) or 2 rows (a batch) per load; the sums are scaled by 1/N
-  // before the epilogue.  (16 rows of 8 columns halves the shared-memory reads of x but
-  // measured 2x slower at N=65536: half the bytes in flight per load.)
+  // before the epilogue.  One trajectory converts the bytes of two rows at a time into a
+  // packed float pair and multiplies it by a column's (cos, cos) and (sin, sin) with packed
+  // FMAs: 2.5 instructions per byte and trajectory instead of 4.  (16 rows of 8 columns
+  // halves the shared-memory reads of x but measured 2x slower at N=65536: half the bytes in
+  // flight per load.)
   __device__ void dense_matvec_i8() {
     constexpr int RG = BMAX == 1 ? 8 : 2;
-    for (int pr0 = r0; pr0 < r1; pr0 += KW * RG) mv_i8_pass<RG, 16>(pr0);
+    for (int pr0 = r0; pr0 < r1; pr0 += KW * RG) {
+      if constexpr (BMAX > 1) mv_i8_pass_batch<RG, 16>(pr0);
+      else mv_i8_pass(pr0);
+    }
   }
 
   // ---- error norm of the attempt (dp45.cu:79-84, 116-119); sum of squares -> rsum[b*PW]

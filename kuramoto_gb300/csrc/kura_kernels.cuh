@@ -10,10 +10,11 @@ constexpr int KT = 512;       // threads per CTA of the persistent integrator
 constexpr int KW = KT / 32;   // warps per CTA
 constexpr int CT = 1024;      // columns per staged x tile of the dense coupling
 constexpr int CT_I8 = 8192;   // the same for int8 rows and one trajectory (16 loads per lane per tile)
-constexpr int CT_F1 = 4096;   // the same for float rows and one trajectory
+constexpr int CT_F1 = 8192;   // the same for float rows and one trajectory
 constexpr int A_ROWS = 4;     // rows per warp and pass of the dense float product
 constexpr int A_STAGES = 3;   // 16-byte chunks per row and lane in flight (cp.async ring) in that product
-constexpr int I8_CHUNK = 18;  // x tile stride of the int8 product per 16 columns, in (cos, sin) pairs
+constexpr int I8_CHUNK4 = 17; // x tile stride of the int8 product per 16 columns, in (cos, cos, sin, sin) float4
+constexpr int I8_CHUNK = 18;  // the same for a batch, in (cos, sin) pairs
 constexpr int F_CHUNK = 6;    // the same for the float product per 4 columns
 constexpr int PW_MAX = 2 * 32 + 2;  // partial sums per trajectory and CTA: 2K projections + (sum cos, sum sin)
 

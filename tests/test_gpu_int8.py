@@ -34,7 +34,7 @@ def test_int8_adjacency_bit_exact(native, oracle_lib, n, k):
     net.close()
 
 
-@pytest.mark.parametrize("n,batch", [(33, 1), (700, 1), (3000, 1), (2000, 8)])
+@pytest.mark.parametrize("n,batch", [(33, 1), (700, 1), (3000, 1), (5000, 1), (21000, 1), (2000, 8)])
 def test_int8_rhs_matches_float32_storage(native, n, batch):
     th, om = cauchy_inputs(n, 9)
     out = []

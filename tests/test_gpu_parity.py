@@ -72,8 +72,10 @@ def test_dense_adjacency_bit_exact(native, oracle_lib, n, k):
 
 # ------------------------------------------------------------------ RHS
 @pytest.mark.parametrize("coupling", [DENSE, VOLCANO])
-@pytest.mark.parametrize("n", [1, 33, 700])
+@pytest.mark.parametrize("n", [1, 33, 700, 5000, 12000])
 def test_rhs_matches_oracle(native, oracle_lib, coupling, n):
+    """Row blocks of 1..79 rows per CTA: warps with 1, 2, 3 and 4 rows of a pass of the dense
+    product, and a second pass."""
     th, om = cauchy_inputs(n, 5)
     th = th + np.float32(40.0) * (np.arange(n) % 3)  # unwrapped phases far from [0, 2pi)
     net = native.Network(n, k=5, coupling=coupling, seed=3)
