@@ -74,8 +74,26 @@ def test_window_inputs_share_trajectory_zero():
     assert not np.array_equal(th4[0], th4[1])
 
 
-def test_volcano_roofline_uses_the_state_bytes():
+def test_volcano_roofline_reports_issue_with_the_state_bytes_beside():
     w = bench.WORKLOADS["volcano200k"]
-    r = bench.roofline(w, dict(kernel_ms=39.9, launches=1, acc_per_step=1023), _args("volcano200k", 1))
-    assert r["bytes_per_unit"] == bench.STATE_BYTES == 150.0
-    assert abs(r["achieved"] - round(150.0 * 1023 * w["n"] / 0.0399 / 1e9, 1)) < 0.11
+    r = bench.roofline(w, dict(kernel_ms=39.9, launches=1, acc_per_step=1023, sms=152,
+                               clocks={"sm_mhz": 2070.0}), _args("volcano200k", 1))
+    # reported against instruction issue; the nominal state-traffic figure rides along
+    assert r["bound"] == "issue"
+    h = r["hbm_nominal"]
+    assert h["bytes_per_unit"] == bench.STATE_BYTES == 150.0
+    assert abs(h["achieved"] - round(150.0 * 1023 * w["n"] / 0.0399 / 1e9, 1)) < 0.11
+    rate = 1023 * w["n"] / 0.0399
+    assert abs(r["frac"] - r["instructions_per_unit"] * rate / (4 * 152 * 2070e6)) < 1e-4
+
+
+def test_issue_roofline_counts_instructions_per_unit():
+    """An issue-bound kernel: warp instructions per accepted oscillator-step (the ncu count in
+    profiles/issue.json) times the rate, over 4 issue slots per SM and cycle."""
+    t = json.load(open(os.path.join(bench.ROOT, "profiles", "issue.json")))["volcano200k"]
+    r = bench.issue_roofline("volcano200k", 5e9, {"sm_mhz": 2000.0}, sms=152)
+    peak = 4 * 152 * 2000e6
+    assert r["bound"] == "issue"
+    assert abs(r["achieved"] - t["warp_instructions_per_accepted_osc_step"] * 5e9 / 1e9) < 0.01
+    assert abs(r["frac"] - t["warp_instructions_per_accepted_osc_step"] * 5e9 / peak) < 1e-4
+    assert bench.issue_roofline("no-such-workload", 5e9, None, sms=152) is None
