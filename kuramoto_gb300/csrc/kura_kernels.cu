@@ -154,9 +154,10 @@ __host__ __device__ inline void smem_layout(int coup, int bmax, int kmax, int ro
                                                    : bmax * ((bmax == 1 ? CT_F1 : CT) / 4) * F_CHUNK * 8);
   // f3 (volcano); for K <= 8 it also holds the table of sum_m +-f3_m over all sign patterns
   off[8] = o; o += align16(coup == KURA_COUPLING_VOLCANO ? (bmax * 2 * kmax * 4 + bmax * 256 * 8) : bmax * 2 * kmax * 4);
-  // own (cos, sin) (volcano); the ring of A chunks in flight (dense float)
+  // own (cos, sin) (volcano); the ring of A chunks in flight (dense float, int8 of one trajectory)
   off[9] = o; o += align16(coup == KURA_COUPLING_VOLCANO && xs_smem ? bmax * rows * 8
-                           : (coup == KURA_COUPLING_DENSE ? KW * A_STAGES * A_ROWS * 32 * 16 : 0));
+                           : coup == KURA_COUPLING_DENSE ? KW * A_STAGES * A_ROWS * 32 * 16
+                           : coup == COUP_DENSE_I8 && bmax == 1 ? KW * I8_SLOTS * 32 * 16 : 0);
   *total = o;
 }
 
@@ -246,7 +247,7 @@ struct Engine {
     nbar = 0;
     xpar = 0;
     xs = pp.xs_smem ? (float2*)(smem + off[9]) : nullptr;
-    ring = (float4*)(smem + off[9]);  // the dense float product's chunks of A in flight
+    ring = (float4*)(smem + off[9]);  // the dense products' chunks of A in flight
   }
 
   // (cos, sin) of row i of trajectory b for the volcano coupling (own rows only)
@@ -927,32 +928,58 @@ struct Engine {
   // the 8 lanes of each phase of a 16-byte shared-memory read on distinct banks.
   static constexpr int CTXP = CTX / 16 * I8_CHUNK4;  // float4 per trajectory
   // The columns [c0, c0 + cw) of the staged tile for the first RGT of the pass's RG_I8 rows of
-  // this warp (rows pr0 + warp + KW*q), CPL int8 columns per lane and load; rows 2qp and 2qp+1
-  // share the packed accumulators acc[qp].  No barrier inside: warps with different RGT run
-  // side by side between the tile barriers of the caller.
+  // this warp (rows pr0 + warp + KW*q), 16 int8 columns per lane and step; rows 2qp and 2qp+1
+  // share the packed accumulators acc[qp].  A streams through the warp's ring of I8_SLOTS
+  // chunk slots (16 bytes per lane) with cp.async, I8_SLOTS / RGT steps deep, so the loads of
+  // the next step are in flight during this step's conversion and FMAs.  No barrier inside:
+  // warps with different RGT run side by side between the tile barriers of the caller.
   static constexpr int RG_I8 = 8;
-  template <int RGT, int CPL>
+  template <int RGT>
   __device__ __forceinline__ void mv_i8_tile(unsigned long long (&acc)[RG_I8 / 2][2], int row0, int c0, int cw) {
-    static_assert(RGT % 2 == 0 && RGT <= RG_I8, "rows are taken in pairs");
-    constexpr int NWD = CPL / 4;
+    static_assert(RGT % 2 == 0 && RGT <= RG_I8 && I8_SLOTS % RGT == 0, "rows are taken in pairs");
+    constexpr int ST = I8_SLOTS / RGT;
     const int ld8 = p.ld8;
     const float4* xt4 = reinterpret_cast<const float4*>(xt);
-    for (int cc = lane * CPL; cc < cw; cc += 32 * CPL) {
-      uint32_t a[RGT][NWD];
+    uint4* my = reinterpret_cast<uint4*>(ring) + (size_t)warp * (I8_SLOTS * 32) + lane;
+    const int8_t* src[RGT];
+    int nb[RGT];
+#pragma unroll
+    for (int q = 0; q < RGT; ++q) {
+      const int row = row0 + KW * q;
+      nb[q] = row < r1 ? 16 : 0;  // rows past the CTA's block are zero-filled
+      src[q] = p.adj8 + (size_t)(row < r1 ? row : r0) * ld8 + c0 + lane * 16;
+    }
+    // steps of this lane: columns cc = lane*16 + 512*it < cw (cw is a multiple of 16)
+    const int nit = cw > lane * 16 ? (cw - lane * 16 + 511) >> 9 : 0;
+#pragma unroll
+    for (int s = 0; s < ST - 1; ++s) {
+      if (s < nit)
+#pragma unroll
+        for (int q = 0; q < RGT; ++q) cp_async16(my + (s * RGT + q) * 32, src[q] + 512 * s, nb[q]);
+      cp_async_commit();
+    }
+    for (int it = 0; it < nit; ++it) {
+      const int ahead = it + ST - 1;
+      if (ahead < nit) {
+        const int sl = ahead % ST;
+#pragma unroll
+        for (int q = 0; q < RGT; ++q) cp_async16(my + (sl * RGT + q) * 32, src[q] + 512 * ahead, nb[q]);
+      }
+      cp_async_commit();
+      cp_async_wait<ST - 1>();  // the chunks of step it have landed
+      const int sl = it % ST;
+      uint32_t a[RGT][4];
 #pragma unroll
       for (int q = 0; q < RGT; ++q) {
-        const int row = row0 + KW * q;
-        const int8_t* src = p.adj8 + (size_t)row * ld8 + c0 + cc;
-        const uint4 v = (row < r1) ? ld_stream_u4(src) : make_uint4(0u, 0u, 0u, 0u);
-        a[q][0] = v.x;
-        a[q][1 % NWD] = v.y;
-        a[q][2 % NWD] = v.z;
-        a[q][3 % NWD] = v.w;
-#pragma unroll
-        for (int wd = 0; wd < NWD; ++wd) a[q][wd] ^= 0x80808080u;
+        const uint4 v = my[(sl * RGT + q) * 32];
+        a[q][0] = v.x ^ 0x80808080u;
+        a[q][1] = v.y ^ 0x80808080u;
+        a[q][2] = v.z ^ 0x80808080u;
+        a[q][3] = v.w ^ 0x80808080u;
       }
+      const int cc = lane * 16 + 512 * it;
 #pragma unroll
-      for (int wd = 0; wd < NWD; ++wd) {
+      for (int wd = 0; wd < 4; ++wd) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           // ((cos, cos), (sin, sin)) of column cc + 4*wd + j
@@ -966,10 +993,10 @@ struct Engine {
         }
       }
     }
+    cp_async_wait<0>();
   }
   // one pass over the RG_I8 rows per warp of one trajectory
   __device__ void mv_i8_pass(int pr0) {
-    constexpr int CPL = 16;
     const int ld = p.ld, ld8 = p.ld8;
     float4* xt4 = reinterpret_cast<float4*>(xt);
     // [qp][0]: (sum k cos) of rows (2qp, 2qp+1); [qp][1]: the same for sin
@@ -989,8 +1016,8 @@ struct Engine {
       __syncthreads();
       // a warp with at most 4 rows in the pass (small N, the last pass) converts no bytes of
       // the absent ones
-      if (nr <= 4) mv_i8_tile<4, CPL>(acc, row0, c0, cw);
-      else mv_i8_tile<RG_I8, CPL>(acc, row0, c0, cw);
+      if (nr <= 4) mv_i8_tile<4>(acc, row0, c0, cw);
+      else mv_i8_tile<RG_I8>(acc, row0, c0, cw);
     }
     float accf[RG_I8][2];
 #pragma unroll

@@ -9,7 +9,8 @@ namespace kura {
 constexpr int KT = 512;       // threads per CTA of the persistent integrator
 constexpr int KW = KT / 32;   // warps per CTA
 constexpr int CT = 1024;      // columns per staged x tile of the dense coupling
-constexpr int CT_I8 = 8192;   // the same for int8 rows and one trajectory (16 loads per lane per tile)
+constexpr int CT_I8 = 4096;   // the same for int8 rows and one trajectory (8 steps of 16 bytes per lane per tile)
+constexpr int I8_SLOTS = 16;  // 16-byte chunk slots per lane in the int8 product's cp.async ring (8 rows x 2 steps)
 constexpr int CT_F1 = 8192;   // the same for float rows and one trajectory
 constexpr int A_ROWS = 4;     // rows per warp and pass of the dense float product
 constexpr int A_STAGES = 3;   // 16-byte chunks per row and lane in flight (cp.async ring) in that product
